@@ -1,0 +1,311 @@
+"""Benchmark of the GB300 SPH step (particle-steps/s).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload dam_break_rigid_1m|dam_break_16k|precision_jet_4m]
+                    [--no-cpu-baseline]
+
+A step is one full two-way step of the scene (hash, stable radix sort, cell
+ranges + sorted gather, density, rigid-sphere grid and fluid->sphere
+contact, pressure+viscosity+walls+contact forces with fused integration,
+FP64 per-body reduction and body integration) -- the reference's
+HeterogeneousSimulator::doTimeStep with its rigid-body coupling.  Default
+workload: 1,048,576 fluid particles + one rigid box of 4,096 surface spheres
+(seeded synthetic scene, no dataset).
+
+`value` times K steps with inputs resident in HBM, each step bracketed by
+CUDA events on the engine's stream and preceded by a 256 MiB write that
+evicts L2 (126 MB).  `e2e` times the same steps through the C ABI with the
+particle state copied from pinned host memory to the device and back inside
+every step.  Under torchrun (N > 1) every rank runs an independent replica
+(the scene does not shard: replicas only), timing is the max over ranks and
+`value` sums all ranks' particle-steps.
+
+--impl reference times the CPU restatement of the reference's path (the
+oracle: the reference's kernel math as OpenMP host loops plus
+RigidBodySimulator's CPU step) on the host cores, rank 0 only.
+"""
+import argparse
+import glob
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLUSH_BYTES = 256 << 20
+BYTES_FORCES = 76   # per particle: sorted pos 16 + sorted vel 16 + density/pressure 8 + id 4 + vel 16 + pos 16
+BYTES_DENSITY = 24  # sorted pos 16 + density/pressure 8
+FLOPS_FORCE_PAIR = 38   # pressure ~17 + viscosity ~15 + accumulate 6, per in-range pair
+FLOPS_DENSITY_PAIR = 11
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max/sum over ranks (gloo on host tensors; no data-path
+    collective exists in this workload)."""
+
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def reduce(self, v, op):
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX if op == "max" else self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel):
+    """DRAM bytes per particle of `kernel` from the committed ncu summary
+    (lines `traffic_bytes_per_particle <kernel> <value>`), or None."""
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.txt"))):
+        with open(path) as f:
+            for ln in f:
+                t = ln.split()
+                if len(t) == 3 and t[0] == "traffic_bytes_per_particle" and t[1] == kernel:
+                    return float(t[2])
+    return None
+
+
+def make_scene(name):
+    from fluidgrid_gb300 import scenes
+    return scenes.WORKLOADS[name]()
+
+
+def cpu_baseline(spec, budget_s=12.0, max_steps=20):
+    """The oracle's FP32 restatement of the reference step on all host cores,
+    on a bounded sample (whole steps of the same workload until ~budget_s)."""
+    from oracle import oracle as O
+    st = O.Stepper(spec)
+    cores = O.max_threads()
+    t0 = time.perf_counter()
+    st.step()
+    done = 1
+    while time.perf_counter() - t0 < budget_s and done < max_steps:
+        st.step()
+        done += 1
+    dt = time.perf_counter() - t0
+    return {"value": spec.n * done / dt, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "sample": "%d full steps of %s (%d particles, %d rigid spheres) in %.1f s" % (
+                done, spec.name, spec.n, spec.nspheres, dt), "pairs_per_step": st.pairs}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    spec = make_scene(args.workload)
+    from oracle import oracle as O
+    st = O.Stepper(spec)
+    for _ in range(args.warmup):
+        st.step()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        st.step()
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    v = spec.n * args.steps / tot
+    line = {"metric": "particle-steps/s", "value": v, "unit": "particle-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": spec.name, "particles": spec.n, "buckets": spec.nbuckets,
+                       "rigid_spheres": spec.nspheres, "bodies": len(spec.bodies)},
+            "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": O.max_threads(), "kind": "port",
+                             "sample": "%d timed full steps after %d warm-up steps" % (args.steps, args.warmup)},
+            "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args, rank, world, local):
+    import fluidgrid_gb300 as fgm
+    from fluidgrid_gb300.world import World, PinnedArray, fp32_peak_tflops
+    from fluidgrid_gb300 import _ffi
+    L = fgm.load()
+    _ffi.check(L.fg_set_device(local), "fg_set_device")
+    dist = Dist(world)
+    spec = make_scene(args.workload)
+    w = World([spec])
+    n = spec.n
+    launches = w.launches_per_step()
+    w.step(args.warmup)
+    w.sync()
+    prof = [w.stage_profile(FLUSH_BYTES) for _ in range(3)]
+    stages = {k: float(np.mean([p[k] for p in prof])) for k in prof[0]}
+    clocks = ClockSampler(local)
+    dist.barrier()
+    w.sync()
+    clocks.start()
+    ms = w.timed_steps(args.steps, FLUSH_BYTES)
+    w.sync()
+    clk = clocks.stop()
+    dist.barrier()
+    total_ms = dist.reduce(float(ms.sum()), "max")
+    w.check_finite()
+    # end to end through host buffers
+    hp, hv = PinnedArray((n, 4)), PinnedArray((n, 4))
+    op, ov = PinnedArray((n, 4)), PinnedArray((n, 4))
+    pos, vel = w.download()
+    hp.array[:] = pos
+    hv.array[:] = vel
+    w.e2e_steps(1, hp.array, hv.array, op.array, ov.array)
+    dist.barrier()
+    ems = w.e2e_steps(args.steps, hp.array, hv.array, op.array, ov.array)
+    dist.barrier()
+    e2e_ms = dist.reduce(float(ems.sum()), "max")
+    for a in (hp, hv, op, ov):
+        a.free()
+    value = world * n * args.steps / (total_ms * 1e-3)
+    e2e_value = world * n * args.steps / (e2e_ms * 1e-3)
+    if rank == 0:
+        peak, peak_kind = measured_peaks()
+        dom = max(("forces", "density"), key=lambda k: stages[k])
+        per_p = BYTES_FORCES if dom == "forces" else BYTES_DENSITY
+        achieved = per_p * n / (stages[dom] * 1e-3) / 1e9
+        tpp = profile_traffic("k_forces" if dom == "forces" else "k_density")
+        cpu = None if args.no_cpu_baseline else cpu_baseline(spec)
+        pairs = cpu["pairs_per_step"] if cpu else None
+        fp32_peak = fp32_peak_tflops()
+        fp32 = None
+        if pairs:
+            flops = (FLOPS_FORCE_PAIR * (pairs - n)) if dom == "forces" else FLOPS_DENSITY_PAIR * pairs
+            ach = flops / (stages[dom] * 1e-3) / 1e12
+            fp32 = {"achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
+                    "pairs_per_step": pairs, "peak_kind": "measured (FMA probe)"}
+        ms_sorted = np.sort(ms)
+        line = {
+            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded jittered lattice + rigid box, seed 0x5EED)",
+            "config": {"workload": spec.name, "particles": n, "buckets": spec.nbuckets,
+                       "rigid_spheres": spec.nspheres, "bodies": len(spec.bodies),
+                       "l2": "flushed before every timed step (256 MiB write)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "latency_ms": {"p50": float(np.percentile(ms_sorted, 50)), "p99": float(np.percentile(ms_sorted, 99))},
+            "stages_ms": stages,
+            "roofline": {"bound": "hbm", "kernel": "k_forces" if dom == "forces" else "k_density",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": (tpp * n) if tpp else None, "peak_kind": peak_kind,
+                         "bytes_per_particle": per_p, "fp32": fp32},
+            "cpu_baseline": ({k: v for k, v in cpu.items() if k != "pairs_per_step"} if cpu else None),
+            "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 32 * n,
+                    "d2h_bytes_per_step": 32 * n},
+            "gpu_launches": launches * args.steps + args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    w.close()
+    dist.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="dam_break_rigid_1m")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,1014 @@
+/* World engine: packed scenes, per-step orchestration, C ABI.
+ *
+ * Host side of the step.  Order per step (one launch per stage for all
+ * scenes), following HeterogeneousSimulator::doTimeStep
+ * (HeterogeneousSimulator.cpp:54-127) and the two-way rigid order of its
+ * commented block with RigidBodySimulator (RigidBodySimulator.cpp:334-611):
+ *   findFluidNeighbourhood  hash, sort, start/end + sorted gather (:131-150)
+ *   calculateFluidDensity   (:153-159)
+ *   generateCollisionData   sphere transform+hash, sort, ranges (:464-474)
+ *   calculateRigidBodyForcesFromFluid (:503-520)
+ *   calculateFluidForces(useDynamicRB) + integrateFluidForces (:161-212),
+ *                           fused into one kernel
+ *   applyForces + integrate (:522-611) as one FP64 kernel per body.
+ * The per-stage device synchronisations of the reference are gone; stages
+ * are stream-ordered and the whole step is replayed from a CUDA graph. */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+#include <stdio.h>
+#include <math.h>
+#include <algorithm>
+#include <string>
+#include <vector>
+#include <mutex>
+#include "fg_types.h"
+#include "fg_kernels.h"
+#include "fg_engine.h"
+#include "fg_device.cuh"
+#include "../../include/fluidgrid_gb300.h"
+
+namespace fg {
+
+static thread_local std::string g_err;
+
+void set_error(const char *what, cudaError_t e)
+{
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+    g_err = buf;
+}
+
+void set_error_msg(const char *what) { g_err = what; }
+
+static uint32_t ceil_log2(uint64_t v)
+{
+    uint32_t b = 0;
+    while ((1ull << b) < v) b++;
+    return b;
+}
+
+static bool is_pow2(uint32_t v) { return v && !(v & (v - 1)); }
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            fg::set_error(#call, e_);                                                                  \
+            return (e_ == cudaErrorMemoryAllocation) ? FG_E_OOM : FG_E_CUDA;                       \
+        }                                                                                          \
+    } while (0)
+
+int World::alloc(void **p, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        set_error("cudaMalloc", e);
+        *p = nullptr;
+        return e == cudaErrorMemoryAllocation ? FG_E_OOM : FG_E_CUDA;
+    }
+    allocs.push_back(*p);
+    device_bytes += bytes;
+    return FG_OK;
+}
+
+World::~World()
+{
+    if (flush_buf) cudaFree(flush_buf);
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (void *p : allocs) cudaFree(p);
+    if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+void fill_scene(FgScene &S, const fg_scene_desc &d)
+{
+    memset(&S, 0, sizeof(S));
+    for (int k = 0; k < 3; k++) S.cell[k] = d.cell_size[k];
+    S.nb = (uint32_t)((int64_t)d.bucket_size[0] * d.bucket_size[1] * d.bucket_size[2]);
+    S.nb_mask = is_pow2(S.nb) ? S.nb - 1 : 0;
+    S.n = d.n_particles;
+    S.h = d.kernel_radius;
+    S.h2 = d.kernel_radius * d.kernel_radius;
+    S.scale = d.simulation_scale;
+    S.dt = d.dt;
+    S.dt_over_scale = d.dt / d.simulation_scale;
+    S.vlimit = d.velocity_limit;
+    for (int k = 0; k < 3; k++) {
+        S.vmin[k] = d.volume_min[k];
+        S.vmax[k] = d.volume_max[k];
+        S.gravity[k] = d.gravity[k];
+        S.noslip_min[k] = d.noslip_min[k];
+        S.noslip_max[k] = d.noslip_max[k];
+    }
+    S.mass = d.mass;
+    S.rest = d.rest_density;
+    S.gas = d.gas_constant;
+    S.visc = d.viscosity;
+    /* KernelsCache, HeterogeneousSimulator.cpp:33-42 (double pow, float store) */
+    const float PI = 3.14159265f;
+    double h = (double)d.kernel_radius;
+    S.kpoly6 = (float)(315.0f / ((double)(64.0f * PI) * pow(h, 9)));
+    S.kspiky = (float)(-(45.0f / ((double)PI * pow(h, 6))));
+    S.kvisc = (float)(45.0f / ((double)PI * pow(h, 6)));
+    S.wall_dist = d.wall_distance;
+    S.wall_stiff = d.wall_stiffness;
+    S.wall_damp = d.wall_damping;
+    S.fric_kin = d.friction_kinetic;
+    S.fric_static = d.friction_static;
+    S.nbodies = d.n_bodies;
+    S.rb_nb = (uint32_t)((int64_t)d.rb_bucket_size[0] * d.rb_bucket_size[1] * d.rb_bucket_size[2]);
+    S.rb_nb_mask = is_pow2(S.rb_nb) ? S.rb_nb - 1 : 0;
+    for (int k = 0; k < 3; k++) {
+        S.rb_cell[k] = d.rb_radius;
+        S.f2r_rel[k] = d.fluid_to_rb_relation[k];
+        S.r2f_rel[k] = d.rb_to_fluid_relation[k];
+        S.rb_vmin[k] = d.rb_volume_min[k];
+        S.rb_vmax[k] = d.rb_volume_max[k];
+    }
+    S.fluid_radius = d.fluid_radius;
+    S.rb_radius = d.rb_radius;
+    S.ck = d.contact_kspring;
+    S.ckd = d.contact_kdamping;
+    S.fluid_eps = d.fluid_contact_eps;
+    S.rb_eps = d.rb_contact_eps;
+    S.rbrb_k = d.rbrb_kspring;
+    S.rbrb_kd = d.rbrb_kdamping;
+    S.rbrb_eps = d.rbrb_eps;
+    for (int k = 0; k < 4; k++) S.rb_gravity[k] = d.rb_gravity[k];
+    S.rb_vlimit = d.rb_velocity_limit;
+    S.rb_dt = d.rb_dt;
+    S.flags = 0;
+    if (d.n_bodies) S.flags |= FG_SCENE_HAS_RB;
+    if (d.rb_rb_contact) S.flags |= FG_SCENE_RB_RB;
+}
+
+int validate(const fg_scene_desc &d)
+{
+    if (d.n_particles && !d.positions) return FG_E_INVALID;
+    for (int k = 0; k < 3; k++) {
+        if (d.bucket_size[k] <= 0) return FG_E_INVALID;
+        if (!(d.cell_size[k] > 0.0f)) return FG_E_INVALID;
+    }
+    int64_t nb = (int64_t)d.bucket_size[0] * d.bucket_size[1] * d.bucket_size[2];
+    if (nb > 0x7fffffffLL) return FG_E_INVALID;
+    if (!(d.kernel_radius > 0.0f) || !(d.simulation_scale != 0.0f)) return FG_E_INVALID;
+    if (d.n_bodies) {
+        if (!d.bodies) return FG_E_INVALID;
+        for (int k = 0; k < 3; k++)
+            if (d.rb_bucket_size[k] <= 0 || d.fluid_to_rb_relation[k] < 0 || d.rb_to_fluid_relation[k] < 0 ||
+                d.fluid_to_rb_relation[k] > 8 || d.rb_to_fluid_relation[k] > 8)
+                return FG_E_INVALID;
+        if (!(d.rb_radius > 0.0f)) return FG_E_INVALID;
+        int64_t rnb = (int64_t)d.rb_bucket_size[0] * d.rb_bucket_size[1] * d.rb_bucket_size[2];
+        if (rnb > 0x7fffffffLL) return FG_E_INVALID;
+        for (uint32_t b = 0; b < d.n_bodies; b++) {
+            if (d.bodies[b].n_spheres && !d.bodies[b].local_spheres) return FG_E_INVALID;
+            if (!(d.bodies[b].mass != 0.0f)) return FG_E_INVALID;
+        }
+    }
+    return FG_OK;
+}
+
+static void build_work(std::vector<FgWork> &wt, uint32_t scene, uint32_t first, uint32_t n)
+{
+    for (uint32_t o = 0; o < n; o += FG_CHUNK) {
+        FgWork w;
+        w.scene = scene;
+        w.first = first + o;
+        w.count = std::min<uint32_t>(FG_CHUNK, n - o);
+        w.pad = 0;
+        wt.push_back(w);
+    }
+}
+
+int World::create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st)
+{
+    nscenes = ns;
+    if (st) {
+        stream = st;
+        own_stream = false;
+    } else {
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        own_stream = true;
+    }
+    scenes_h.resize(ns);
+    uint64_t np = 0, nbk = 0, nsph = 0, nbod = 0, nrbk = 0;
+    for (uint32_t s = 0; s < ns; s++) {
+        int v = validate(d[s]);
+        if (v != FG_OK) {
+            set_error_msg("invalid scene description");
+            return v;
+        }
+        FgScene &S = scenes_h[s];
+        fill_scene(S, d[s]);
+        S.pbase = (uint32_t)np;
+        S.bucket_base = (uint32_t)nbk;
+        S.sph_base = (uint32_t)nsph;
+        S.body_base = (uint32_t)nbod;
+        S.rb_bucket_base = (uint32_t)nrbk;
+        uint64_t sph = 0;
+        for (uint32_t b = 0; b < d[s].n_bodies; b++) sph += d[s].bodies[b].n_spheres;
+        S.nsph = (uint32_t)sph;
+        np += d[s].n_particles;
+        nbk += S.nb;
+        nsph += sph;
+        nbod += d[s].n_bodies;
+        if (d[s].n_bodies) nrbk += S.rb_nb;
+    }
+    if (np >= 0x7fffffffULL || nbk >= 0x7fffffffULL || nsph >= 0x7fffffffULL || nrbk >= 0x7fffffffULL) {
+        set_error_msg("world too large");
+        return FG_E_INVALID;
+    }
+    n = (uint32_t)np;
+    total_buckets = (uint32_t)nbk;
+    nspheres = (uint32_t)nsph;
+    nbodies = (uint32_t)nbod;
+    total_rb_buckets = (uint32_t)nrbk;
+    key_bits = ceil_log2(total_buckets);
+    rb_key_bits = ceil_log2(std::max<uint32_t>(total_rb_buckets, 1));
+    digit_bits = key_bits <= 16 ? std::max<uint32_t>(1, (key_bits + 1) / 2) : (key_bits + 2) / 3;
+    if (digit_bits > 8) digit_bits = 8;
+
+    /* work tables */
+    std::vector<FgWork> fw, sw;
+    for (uint32_t s = 0; s < ns; s++) {
+        build_work(fw, s, scenes_h[s].pbase, scenes_h[s].n);
+        build_work(sw, s, scenes_h[s].sph_base, scenes_h[s].nsph);
+    }
+    nwork = (uint32_t)fw.size();
+    nwork_sph = (uint32_t)sw.size();
+    single = (ns == 1);
+
+    int r;
+    auto A = [&](void **p, size_t b) { return alloc(p, b); };
+    if ((r = A((void **)&scenes_d, sizeof(FgScene) * std::max<uint32_t>(ns, 1)))) return r;
+    if ((r = A((void **)&work_d, sizeof(FgWork) * std::max<uint32_t>(nwork, 1)))) return r;
+    if ((r = A((void **)&work_sph_d, sizeof(FgWork) * std::max<uint32_t>(nwork_sph, 1)))) return r;
+    const size_t N = std::max<uint32_t>(n, 1);
+    if ((r = A((void **)&pos, 16 * N))) return r;
+    if ((r = A((void **)&vel, 16 * N))) return r;
+    if ((r = A((void **)&keys_u, 4 * N))) return r;
+    if ((r = A((void **)&keys, 4 * N))) return r;
+    if ((r = A((void **)&ids, 4 * N))) return r;
+    if ((r = A((void **)&spos, 16 * N))) return r;
+    if ((r = A((void **)&svel, 16 * N))) return r;
+    if ((r = A((void **)&dp, 8 * N))) return r;
+    if ((r = A((void **)&start, 4 * (size_t)std::max<uint32_t>(total_buckets, 1)))) return r;
+    if ((r = A((void **)&end, 4 * (size_t)std::max<uint32_t>(total_buckets, 1)))) return r;
+    const size_t M = std::max(N, (size_t)std::max<uint32_t>(nspheres, 1));
+    if ((r = A((void **)&rs.keys_alt, 4 * M))) return r;
+    if ((r = A((void **)&rs.vals_alt, 4 * M))) return r;
+    if ((r = A((void **)&rs.hist, 4 * radix_hist_words((uint32_t)M)))) return r;
+    if ((r = A((void **)&status_d, 64))) return r;
+    CK(cudaMemsetAsync(status_d, 0, 64, stream));
+    CK(cudaMemsetAsync(dp, 0, 8 * N, stream));
+    CK(cudaMemsetAsync(vel, 0, 16 * N, stream));
+    CK(cudaMemsetAsync(end, 0, 4 * (size_t)std::max<uint32_t>(total_buckets, 1), stream));
+
+    if (nbodies) {
+        const size_t S = std::max<uint32_t>(nspheres, 1), B = nbodies;
+        if ((r = A((void **)&rb_local, 16 * S))) return r;
+        if ((r = A((void **)&rb_world, 16 * S))) return r;
+        if ((r = A((void **)&rb_keys_u, 4 * S))) return r;
+        if ((r = A((void **)&rb_keys, 4 * S))) return r;
+        if ((r = A((void **)&rb_ids, 4 * S))) return r;
+        if ((r = A((void **)&rb_spos, 16 * S))) return r;
+        if ((r = A((void **)&rb_force, 16 * S))) return r;
+        if ((r = A((void **)&rb_torque, 16 * S))) return r;
+        if ((r = A((void **)&rb_start, 4 * (size_t)std::max<uint32_t>(total_rb_buckets, 1)))) return r;
+        if ((r = A((void **)&rb_end, 4 * (size_t)std::max<uint32_t>(total_rb_buckets, 1)))) return r;
+        if ((r = A((void **)&aabb, 24 * (size_t)ns))) return r;
+        if ((r = A((void **)&bx, 32 * B))) return r;
+        if ((r = A((void **)&bv, 32 * B))) return r;
+        if ((r = A((void **)&bq, 32 * B))) return r;
+        if ((r = A((void **)&bL, 32 * B))) return r;
+        if ((r = A((void **)&bfs, 32 * B))) return r;
+        if ((r = A((void **)&bts, 32 * B))) return r;
+        if ((r = A((void **)&bxf, 16 * B))) return r;
+        if ((r = A((void **)&bvf, 16 * B))) return r;
+        if ((r = A((void **)&bqf, 16 * B))) return r;
+        if ((r = A((void **)&bmass, 8 * B))) return r;
+        if ((r = A((void **)&binv, 72 * B))) return r;
+        if ((r = A((void **)&body_scene, 4 * B))) return r;
+        if ((r = A((void **)&body_first, 4 * B))) return r;
+        if ((r = A((void **)&body_count, 4 * B))) return r;
+        CK(cudaMemsetAsync(rb_end, 0, 4 * (size_t)std::max<uint32_t>(total_rb_buckets, 1), stream));
+        /* host staging of bodies */
+        std::vector<float> local(4 * S, 0.0f);
+        std::vector<double> hx(4 * B), hv(4 * B, 0.0), hq(4 * B), hL(4 * B, 0.0), hm(B), hinv(9 * B);
+        std::vector<float> hxf(4 * B), hvf(4 * B, 0.0f), hqf(4 * B);
+        std::vector<uint32_t> hbs(B), hbf(B), hbc(B);
+        uint32_t gb = 0, gs = 0;
+        for (uint32_t s = 0; s < ns; s++)
+            for (uint32_t b = 0; b < d[s].n_bodies; b++, gb++) {
+                const fg_body_desc &bd = d[s].bodies[b];
+                hbs[gb] = s;
+                hbf[gb] = gs;
+                hbc[gb] = bd.n_spheres;
+                for (uint32_t k = 0; k < bd.n_spheres; k++, gs++) {
+                    local[4 * gs + 0] = bd.local_spheres[4 * k + 0];
+                    local[4 * gs + 1] = bd.local_spheres[4 * k + 1];
+                    local[4 * gs + 2] = bd.local_spheres[4 * k + 2];
+                    local[4 * gs + 3] = (float)gb; /* w = global body index */
+                }
+                for (int c = 0; c < 3; c++) hx[4 * gb + c] = bd.position[c];
+                hx[4 * gb + 3] = 0.0;
+                for (int c = 0; c < 4; c++) hq[4 * gb + c] = bd.orientation[c];
+                hm[gb] = bd.mass;
+                for (int c = 0; c < 9; c++) hinv[9 * gb + c] = bd.inv_inertia[c];
+                for (int c = 0; c < 4; c++) {
+                    hxf[4 * gb + c] = (float)hx[4 * gb + c];
+                    hqf[4 * gb + c] = (float)hq[4 * gb + c];
+                }
+            }
+        CK(cudaMemcpy(rb_local, local.data(), 16 * (size_t)nspheres, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bx, hx.data(), 32 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bv, hv.data(), 32 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bq, hq.data(), 32 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bL, hL.data(), 32 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bxf, hxf.data(), 16 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bvf, hvf.data(), 16 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bqf, hqf.data(), 16 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bmass, hm.data(), 8 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(binv, hinv.data(), 72 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(body_scene, hbs.data(), 4 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(body_first, hbf.data(), 4 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(body_count, hbc.data(), 4 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemsetAsync(bfs, 0, 32 * B, stream));
+        CK(cudaMemsetAsync(bts, 0, 32 * B, stream));
+    }
+    CK(cudaMemcpy(scenes_d, scenes_h.data(), sizeof(FgScene) * ns, cudaMemcpyHostToDevice));
+    if (nwork) CK(cudaMemcpy(work_d, fw.data(), sizeof(FgWork) * nwork, cudaMemcpyHostToDevice));
+    if (nwork_sph) CK(cudaMemcpy(work_sph_d, sw.data(), sizeof(FgWork) * nwork_sph, cudaMemcpyHostToDevice));
+
+    /* initial state */
+    for (uint32_t s = 0; s < ns; s++) {
+        const FgScene &S = scenes_h[s];
+        if (!S.n) continue;
+        CK(cudaMemcpy(pos + S.pbase, d[s].positions, 16 * (size_t)S.n, cudaMemcpyHostToDevice));
+        if (d[s].velocities)
+            CK(cudaMemcpy(vel + S.pbase, d[s].velocities, 16 * (size_t)S.n, cudaMemcpyHostToDevice));
+    }
+    CK(cudaStreamSynchronize(stream));
+    return FG_OK;
+}
+
+Launch World::fluid_launch() const
+{
+    Launch L;
+    L.table = single ? nullptr : scenes_d;
+    L.single = &scenes_h[0];
+    L.work = single ? nullptr : work_d;
+    L.nwork = nwork;
+    L.n = n;
+    L.stream = stream;
+    return L;
+}
+
+Launch World::sphere_launch() const
+{
+    Launch L;
+    L.table = single ? nullptr : scenes_d;
+    L.single = &scenes_h[0];
+    L.work = single ? nullptr : work_sph_d;
+    L.nwork = nwork_sph;
+    L.n = nspheres;
+    L.stream = stream;
+    return L;
+}
+
+/* Ordered-int AABB reset: mins to +big, maxes to -big. */
+__global__ void k_aabb_reset(int *aabb, uint32_t ns)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 6 * ns) aabb[i] = (i % 6) < 3 ? fg_float_ord(3.0e38f) : fg_float_ord(-3.0e38f);
+}
+
+uint32_t World::enqueue_step(cudaEvent_t *ev)
+{
+    /* ev: optional 16 events, (2k, 2k+1) bracket stage bit k */
+    auto mark = [&](int k, int end_) {
+        if (ev) cudaEventRecord(ev[2 * k + end_], stream);
+    };
+    uint32_t launches = 0;
+    const Launch L = fluid_launch();
+    if (stages & FG_STAGE_HASH) {
+        mark(0, 0);
+        launch_hash(L, pos, keys_u, nullptr);
+        mark(0, 1);
+        launches++;
+    }
+    if (stages & FG_STAGE_SORT) {
+        mark(1, 0);
+        radix_sort(keys_u, nullptr, keys, ids, n, key_bits, digit_bits, rs, stream);
+        mark(1, 1);
+        launches += 3 * radix_passes(key_bits, digit_bits);
+    }
+    if (stages & FG_STAGE_RANGES) {
+        mark(2, 0);
+        cudaMemsetAsync(start, 0xff, 4 * (size_t)total_buckets, stream);
+        launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream);
+        mark(2, 1);
+        launches += 1;
+    }
+    if (stages & FG_STAGE_DENSITY) {
+        mark(3, 0);
+        launch_density(L, spos, start, end, dp, 0.f, 0.f, 0.f, 0);
+        mark(3, 1);
+        launches++;
+    }
+    const bool rb = nbodies > 0;
+    const Launch Ls = sphere_launch();
+    if (rb && (stages & FG_STAGE_RB_GRID)) {
+        mark(4, 0);
+        k_aabb_reset<<<(6 * nscenes + 127) / 128, 128, 0, stream>>>(aabb, nscenes);
+        launch_hash_with_offset(Ls, rb_local, bxf, bqf, rb_world, rb_keys_u, nullptr, aabb);
+        radix_sort(rb_keys_u, nullptr, rb_keys, rb_ids, nspheres, rb_key_bits, 8, rs, stream);
+        cudaMemsetAsync(rb_start, 0xff, 4 * (size_t)total_rb_buckets, stream);
+        launch_cell_ranges(rb_keys, rb_ids, rb_world, nullptr, rb_start, rb_end, rb_spos, nullptr, nspheres, stream);
+        mark(4, 1);
+        launches += 3 + 3 * radix_passes(rb_key_bits, 8);
+    }
+    if (rb && (stages & FG_STAGE_RB_CONTACT)) {
+        mark(5, 0);
+        launch_rb_from_fluid(Ls, rb_spos, rb_ids, bvf, bxf, spos, svel, start, end, rb_force, rb_torque, 0);
+        launches++;
+        if (any_rb_rb) {
+            launch_rb_from_rb(Ls, rb_spos, rb_ids, bvf, bxf, rb_start, rb_end, rb_force, rb_torque, nullptr, 1);
+            launches++;
+        }
+        mark(5, 1);
+    }
+    if (stages & FG_STAGE_FORCES) {
+        mark(6, 0);
+        RigidGrid G;
+        G.spos = rb_spos;
+        G.start = rb_start;
+        G.end = rb_end;
+        G.body_vel = bvf;
+        G.aabb = aabb;
+        G.own_geometry = 0;
+        G.nb = 0;
+        G.mask = 0;
+        ForceOut o;
+        o.vel = vel;
+        o.pos = fused_integrate ? pos : nullptr;
+        launch_forces(L, spos, svel, dp, start, end, ids, o, rb ? &G : nullptr, nullptr, 0.f, 0.f, 0);
+        launches++;
+        if (!fused_integrate) {
+            launch_integrate(L, pos, vel);
+            launches++;
+        }
+        mark(6, 1);
+    }
+    if (rb && (stages & FG_STAGE_BODIES)) {
+        mark(7, 0);
+        BodyState b;
+        b.x = bx; b.v = bv; b.q = bq; b.L = bL;
+        b.inv_inertia = binv;
+        b.mass = bmass;
+        b.x_f = bxf; b.v_f = bvf; b.q_f = bqf;
+        b.force_sum = bfs; b.torque_sum = bts;
+        launch_body_update(single ? nullptr : scenes_d, &scenes_h[0], body_scene, body_first, body_count, nbodies,
+                           rb_force, rb_torque, b, 1, stream);
+        mark(7, 1);
+        launches++;
+    }
+    return launches;
+}
+
+int World::step(uint32_t nsteps)
+{
+    if (!use_graphs) {
+        for (uint32_t k = 0; k < nsteps; k++) enqueue_step();
+        cudaError_t e = cudaPeekAtLastError();
+        if (e != cudaSuccess) {
+            set_error("step", e);
+            return FG_E_CUDA;
+        }
+        return FG_OK;
+    }
+    if (!graph_exec || graph_stages != stages || graph_fused != fused_integrate || graph_digits != digit_bits) {
+        if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+        if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+        CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_step();
+        cudaError_t e = cudaStreamEndCapture(stream, &graph);
+        if (e != cudaSuccess) {
+            set_error("cudaStreamEndCapture", e);
+            return FG_E_CUDA;
+        }
+        CK(cudaGraphInstantiate(&graph_exec, graph, 0));
+        graph_stages = stages;
+        graph_fused = fused_integrate;
+        graph_digits = digit_bits;
+    }
+    for (uint32_t k = 0; k < nsteps; k++) CK(cudaGraphLaunch(graph_exec, stream));
+    return FG_OK;
+}
+
+uint32_t World::launches_per_step()
+{
+    /* count by enqueueing into a capture-free dry description */
+    uint32_t c = 0;
+    if (stages & FG_STAGE_HASH) c += 1;
+    if (stages & FG_STAGE_SORT) c += 3 * radix_passes(key_bits, digit_bits);
+    if (stages & FG_STAGE_RANGES) c += 1; /* + one memset node */
+    if (stages & FG_STAGE_DENSITY) c += 1;
+    if (nbodies) {
+        if (stages & FG_STAGE_RB_GRID) c += 3 + 3 * radix_passes(rb_key_bits, 8); /* aabb reset, hash, ranges */
+        if (stages & FG_STAGE_RB_CONTACT) c += 1 + (any_rb_rb ? 1 : 0);
+        if (stages & FG_STAGE_BODIES) c += 1;
+    }
+    if (stages & FG_STAGE_FORCES) c += fused_integrate ? 1 : 2;
+    return c;
+}
+
+/* NaN/Inf scan of positions and velocities */
+__global__ void k_check(const float4 *pos, const float4 *vel, uint32_t n, uint32_t *status)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 p = pos[i], v = vel[i];
+        if (!isfinite(p.x) || !isfinite(p.y) || !isfinite(p.z) || !isfinite(v.x) || !isfinite(v.y) ||
+            !isfinite(v.z))
+            atomicOr(status, FG_DEV_NONFINITE);
+    }
+}
+
+int World::check()
+{
+    if (!n) return FG_OK;
+    k_check<<<grid_for((n + 255) / 256, 8), 256, 0, stream>>>(pos, vel, n, status_d);
+    return FG_OK;
+}
+
+int World::sync()
+{
+    CK(cudaStreamSynchronize(stream));
+    uint32_t st = 0;
+    CK(cudaMemcpy(&st, status_d, 4, cudaMemcpyDeviceToHost));
+    if (st & FG_DEV_NONFINITE) return FG_E_NONFINITE;
+    return FG_OK;
+}
+
+/* RAII event set */
+struct Events {
+    std::vector<cudaEvent_t> ev;
+    explicit Events(size_t n) : ev(n, nullptr)
+    {
+        for (auto &e : ev) cudaEventCreate(&e);
+    }
+    ~Events()
+    {
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
+int World::ensure_flush(size_t bytes)
+{
+    if (bytes <= flush_bytes) return FG_OK;
+    if (flush_buf) cudaFree(flush_buf);
+    flush_buf = nullptr;
+    flush_bytes = 0;
+    CK(cudaMalloc(&flush_buf, bytes));
+    flush_bytes = bytes;
+    return FG_OK;
+}
+
+int World::stage_profile(size_t fbytes, float *ms)
+{
+    Events E(16);
+    for (int k = 0; k < 16; k++)
+        if (!E.ev[k]) return FG_E_CUDA;
+    if (fbytes) {
+        int r = ensure_flush(fbytes);
+        if (r != FG_OK) return r;
+        launch_fill(flush_buf, fbytes / 4, 7u, stream);
+    }
+    for (int k = 0; k < 8; k++) ms[k] = 0.0f;
+    enqueue_step(E.ev.data());
+    CK(cudaStreamSynchronize(stream));
+    for (int k = 0; k < 8; k++) {
+        if (cudaEventQuery(E.ev[2 * k]) != cudaSuccess || cudaEventQuery(E.ev[2 * k + 1]) != cudaSuccess) {
+            cudaGetLastError(); /* stage not run: events never recorded */
+            continue;
+        }
+        float t = 0.0f;
+        if (cudaEventElapsedTime(&t, E.ev[2 * k], E.ev[2 * k + 1]) == cudaSuccess) ms[k] = t;
+        else cudaGetLastError();
+    }
+    return FG_OK;
+}
+
+int World::timed_steps(uint32_t nsteps, size_t fbytes, float *ms)
+{
+    if (fbytes) {
+        int r = ensure_flush(fbytes);
+        if (r != FG_OK) return r;
+    }
+    Events E(2 * (size_t)nsteps);
+    for (uint32_t k = 0; k < nsteps; k++) {
+        if (fbytes) launch_fill(flush_buf, fbytes / 4, k, stream);
+        CK(cudaEventRecord(E.ev[2 * k], stream));
+        int r = step(1);
+        if (r != FG_OK) return r;
+        CK(cudaEventRecord(E.ev[2 * k + 1], stream));
+    }
+    CK(cudaStreamSynchronize(stream));
+    for (uint32_t k = 0; k < nsteps; k++) CK(cudaEventElapsedTime(&ms[k], E.ev[2 * k], E.ev[2 * k + 1]));
+    return FG_OK;
+}
+
+int World::e2e_steps(uint32_t nsteps, const float *hp, const float *hv, float *op, float *ov, float *ms)
+{
+    Events E(2 * (size_t)nsteps);
+    const size_t b = 16 * (size_t)n;
+    for (uint32_t k = 0; k < nsteps; k++) {
+        CK(cudaEventRecord(E.ev[2 * k], stream));
+        if (b) {
+            CK(cudaMemcpyAsync(pos, hp, b, cudaMemcpyHostToDevice, stream));
+            CK(cudaMemcpyAsync(vel, hv, b, cudaMemcpyHostToDevice, stream));
+        }
+        int r = step(1);
+        if (r != FG_OK) return r;
+        if (b) {
+            CK(cudaMemcpyAsync(op, pos, b, cudaMemcpyDeviceToHost, stream));
+            CK(cudaMemcpyAsync(ov, vel, b, cudaMemcpyDeviceToHost, stream));
+        }
+        CK(cudaEventRecord(E.ev[2 * k + 1], stream));
+    }
+    CK(cudaStreamSynchronize(stream));
+    for (uint32_t k = 0; k < nsteps; k++) CK(cudaEventElapsedTime(&ms[k], E.ev[2 * k], E.ev[2 * k + 1]));
+    return FG_OK;
+}
+
+/* Register-resident FMA loop: 8 independent chains per thread. */
+__global__ void k_fma_probe(float *out, int iters, float a, float b)
+{
+    float x0 = threadIdx.x * 1e-7f, x1 = x0 + 1e-7f, x2 = x0 + 2e-7f, x3 = x0 + 3e-7f;
+    float x4 = x0 + 4e-7f, x5 = x0 + 5e-7f, x6 = x0 + 6e-7f, x7 = x0 + 7e-7f;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+            x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+        }
+    }
+    float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == 12345.678f) out[0] = s; /* keeps the loop alive */
+}
+
+int probe_fp32(float *tflops)
+{
+    float *d = nullptr;
+    CK(cudaMalloc(&d, 16));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = sm_count() * 8, threads = 256, iters = 4096;
+    k_fma_probe<<<blocks, threads>>>(d, 64, 0.999f, 1e-6f); /* warm-up */
+    cudaEventRecord(e0);
+    k_fma_probe<<<blocks, threads>>>(d, iters, 0.999f, 1e-6f);
+    cudaEventRecord(e1);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        set_error("fp32 probe", e);
+        return FG_E_CUDA;
+    }
+    double flops = 2.0 * 8.0 * 16.0 * (double)iters * (double)blocks * (double)threads;
+    *tflops = (float)(flops / (ms * 1e-3) / 1e12);
+    return FG_OK;
+}
+
+} // namespace fg
+
+/* ============================================================ C ABI */
+
+using fg::World;
+
+extern "C" {
+
+void fg_scene_desc_defaults(fg_scene_desc *d)
+{
+    if (!d) return;
+    memset(d, 0, sizeof(*d));
+    const float h = 0.0457f;
+    for (int k = 0; k < 3; k++) {
+        d->cell_size[k] = h;
+        d->bucket_size[k] = 64;
+        d->volume_min[k] = 0.0f;
+        d->volume_max[k] = 1.0f;
+        d->rb_bucket_size[k] = 64;
+        d->fluid_to_rb_relation[k] = 1;
+        d->rb_to_fluid_relation[k] = 1;
+        d->rb_volume_min[k] = 0.0f;
+        d->rb_volume_max[k] = 1.0f;
+    }
+    d->gravity[1] = -9.8f;
+    d->kernel_radius = h;
+    d->velocity_limit = 600.0f;
+    d->simulation_scale = 1.0f;
+    d->dt = 0.003f;
+    d->mass = 0.02f;
+    d->rest_density = 998.29f;
+    d->gas_constant = 3.0f;
+    d->viscosity = 3.5f;
+    /* SPHCalculateForcesK literals (K_FluidSim.cu:289-293) */
+    d->wall_distance = 0.003043174f;
+    d->wall_stiffness = 20000.0f;
+    d->wall_damping = 256.0f;
+    d->noslip_min[0] = -11.0f; d->noslip_min[1] = -40.0f; d->noslip_min[2] = -11.0f;
+    d->noslip_max[0] = 11.0f; d->noslip_max[1] = 200.0f; d->noslip_max[2] = 11.0f;
+    d->friction_kinetic = 0.0f;
+    d->friction_static = 0.0f;
+    d->fluid_radius = 0.25f * h;
+    d->rb_radius = 0.5f * h;
+    d->contact_kspring = -10.0f; /* HeterogeneousSimulator.cpp:180 */
+    d->contact_kdamping = -5.0f;
+    d->fluid_contact_eps = 0.003f;
+    d->rb_contact_eps = 0.0001f;
+    d->rbrb_kspring = -10.0f;
+    d->rbrb_kdamping = -5.0f;
+    d->rbrb_eps = 0.001f;
+    d->rb_gravity[1] = -9.8f;
+    d->rb_velocity_limit = 600.0f;
+    d->rb_dt = 0.003f;
+}
+
+int fg_world_create(const fg_scene_desc *scenes, uint32_t nscenes, fg_stream_t stream, fg_world **out)
+{
+    if (!out || !scenes || nscenes == 0) return FG_E_INVALID;
+    *out = nullptr;
+    for (uint32_t s = 0; s < nscenes; s++) {
+        int v = fg::validate(scenes[s]);
+        if (v != FG_OK) {
+            fg::set_error_msg("invalid scene description");
+            return v;
+        }
+    }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        fg::set_error("cudaGetDeviceCount", e == cudaSuccess ? cudaErrorNoDevice : e);
+        return FG_E_NOLIB;
+    }
+    World *w = new World();
+    int r = w->create(scenes, nscenes, (cudaStream_t)stream);
+    if (r != FG_OK) {
+        delete w;
+        return r;
+    }
+    for (uint32_t s = 0; s < nscenes; s++)
+        if (scenes[s].n_bodies && scenes[s].rb_rb_contact) w->any_rb_rb = true;
+    *out = (fg_world *)w;
+    return FG_OK;
+}
+
+int fg_world_destroy(fg_world *w)
+{
+    if (!w) return FG_E_INVALID;
+    World *W = (World *)w;
+    cudaStreamSynchronize(W->stream);
+    delete W;
+    return FG_OK;
+}
+
+int fg_world_step(fg_world *w, uint32_t nsteps)
+{
+    if (!w) return FG_E_INVALID;
+    return ((World *)w)->step(nsteps);
+}
+
+int fg_world_sync(fg_world *w)
+{
+    if (!w) return FG_E_INVALID;
+    return ((World *)w)->sync();
+}
+
+int fg_world_check(fg_world *w)
+{
+    if (!w) return FG_E_INVALID;
+    return ((World *)w)->check();
+}
+
+int fg_world_upload(fg_world *w, const float *pos4, const float *vel4)
+{
+    if (!w) return FG_E_INVALID;
+    World *W = (World *)w;
+    if (!W->n) return FG_OK;
+    if (pos4) CK(cudaMemcpyAsync(W->pos, pos4, 16 * (size_t)W->n, cudaMemcpyHostToDevice, W->stream));
+    if (vel4) CK(cudaMemcpyAsync(W->vel, vel4, 16 * (size_t)W->n, cudaMemcpyHostToDevice, W->stream));
+    return FG_OK;
+}
+
+int fg_world_download(fg_world *w, float *pos4, float *vel4)
+{
+    if (!w) return FG_E_INVALID;
+    World *W = (World *)w;
+    if (!W->n) return FG_OK;
+    if (pos4) CK(cudaMemcpyAsync(pos4, W->pos, 16 * (size_t)W->n, cudaMemcpyDeviceToHost, W->stream));
+    if (vel4) CK(cudaMemcpyAsync(vel4, W->vel, 16 * (size_t)W->n, cudaMemcpyDeviceToHost, W->stream));
+    return FG_OK;
+}
+
+int fg_world_scene_upload(fg_world *w, uint32_t scene, const float *pos4, const float *vel4)
+{
+    if (!w) return FG_E_INVALID;
+    World *W = (World *)w;
+    if (scene >= W->nscenes) return FG_E_INVALID;
+    const FgScene &S = W->scenes_h[scene];
+    if (!S.n) return FG_OK;
+    if (pos4) CK(cudaMemcpyAsync(W->pos + S.pbase, pos4, 16 * (size_t)S.n, cudaMemcpyHostToDevice, W->stream));
+    if (vel4) CK(cudaMemcpyAsync(W->vel + S.pbase, vel4, 16 * (size_t)S.n, cudaMemcpyHostToDevice, W->stream));
+    return FG_OK;
+}
+
+int fg_world_scene_download(fg_world *w, uint32_t scene, float *pos4, float *vel4)
+{
+    if (!w) return FG_E_INVALID;
+    World *W = (World *)w;
+    if (scene >= W->nscenes) return FG_E_INVALID;
+    const FgScene &S = W->scenes_h[scene];
+    if (!S.n) return FG_OK;
+    if (pos4) CK(cudaMemcpyAsync(pos4, W->pos + S.pbase, 16 * (size_t)S.n, cudaMemcpyDeviceToHost, W->stream));
+    if (vel4) CK(cudaMemcpyAsync(vel4, W->vel + S.pbase, 16 * (size_t)S.n, cudaMemcpyDeviceToHost, W->stream));
+    return FG_OK;
+}
+
+uint32_t fg_world_particles(const fg_world *w) { return w ? ((const World *)w)->n : 0; }
+uint32_t fg_world_scenes(const fg_world *w) { return w ? ((const World *)w)->nscenes : 0; }
+uint32_t fg_world_spheres(const fg_world *w) { return w ? ((const World *)w)->nspheres : 0; }
+uint32_t fg_world_bodies(const fg_world *w) { return w ? ((const World *)w)->nbodies : 0; }
+
+int fg_world_scene_layout(const fg_world *w, uint32_t scene, uint32_t out[8])
+{
+    if (!w || !out) return FG_E_INVALID;
+    const World *W = (const World *)w;
+    if (scene >= W->nscenes) return FG_E_INVALID;
+    const FgScene &S = W->scenes_h[scene];
+    out[0] = S.pbase; out[1] = S.n; out[2] = S.bucket_base; out[3] = S.nb;
+    out[4] = S.sph_base; out[5] = S.nsph; out[6] = S.body_base; out[7] = S.nbodies;
+    return FG_OK;
+}
+
+int fg_world_buffer(fg_world *w, int id, void **dev_ptr, size_t *bytes)
+{
+    if (!w || !dev_ptr || !bytes) return FG_E_INVALID;
+    World *W = (World *)w;
+    const size_t N = W->n, B = W->total_buckets, S = W->nspheres, RB = W->total_rb_buckets, NB = W->nbodies;
+    void *p = nullptr;
+    size_t b = 0;
+    switch (id) {
+    case FG_BUF_POS: p = W->pos; b = 16 * N; break;
+    case FG_BUF_VEL: p = W->vel; b = 16 * N; break;
+    case FG_BUF_KEYS_UNSORTED: p = W->keys_u; b = 4 * N; break;
+    case FG_BUF_KEYS: p = W->keys; b = 4 * N; break;
+    case FG_BUF_IDS: p = W->ids; b = 4 * N; break;
+    case FG_BUF_START: p = W->start; b = 4 * B; break;
+    case FG_BUF_END: p = W->end; b = 4 * B; break;
+    case FG_BUF_SPOS: p = W->spos; b = 16 * N; break;
+    case FG_BUF_SVEL: p = W->svel; b = 16 * N; break;
+    case FG_BUF_DP: p = W->dp; b = 8 * N; break;
+    case FG_BUF_RB_LOCAL: p = W->rb_local; b = 16 * S; break;
+    case FG_BUF_RB_WORLD: p = W->rb_world; b = 16 * S; break;
+    case FG_BUF_RB_KEYS_UNSORTED: p = W->rb_keys_u; b = 4 * S; break;
+    case FG_BUF_RB_KEYS: p = W->rb_keys; b = 4 * S; break;
+    case FG_BUF_RB_IDS: p = W->rb_ids; b = 4 * S; break;
+    case FG_BUF_RB_START: p = W->rb_start; b = 4 * RB; break;
+    case FG_BUF_RB_END: p = W->rb_end; b = 4 * RB; break;
+    case FG_BUF_RB_SPOS: p = W->rb_spos; b = 16 * S; break;
+    case FG_BUF_RB_FORCE: p = W->rb_force; b = 16 * S; break;
+    case FG_BUF_RB_TORQUE: p = W->rb_torque; b = 16 * S; break;
+    case FG_BUF_BODY_X: p = W->bx; b = 32 * NB; break;
+    case FG_BUF_BODY_V: p = W->bv; b = 32 * NB; break;
+    case FG_BUF_BODY_Q: p = W->bq; b = 32 * NB; break;
+    case FG_BUF_BODY_L: p = W->bL; b = 32 * NB; break;
+    case FG_BUF_BODY_FSUM: p = W->bfs; b = 32 * NB; break;
+    case FG_BUF_BODY_TSUM: p = W->bts; b = 32 * NB; break;
+    case FG_BUF_BODY_XF: p = W->bxf; b = 16 * NB; break;
+    case FG_BUF_BODY_VF: p = W->bvf; b = 16 * NB; break;
+    case FG_BUF_BODY_QF: p = W->bqf; b = 16 * NB; break;
+    case FG_BUF_BODY_MASS: p = W->bmass; b = 8 * NB; break;
+    case FG_BUF_BODY_INV_INERTIA: p = W->binv; b = 72 * NB; break;
+    default: return FG_E_INVALID;
+    }
+    *dev_ptr = p;
+    *bytes = p ? b : 0;
+    return FG_OK;
+}
+
+int fg_world_set_stages(fg_world *w, uint32_t mask)
+{
+    if (!w) return FG_E_INVALID;
+    ((World *)w)->stages = mask & FG_STAGE_ALL;
+    return FG_OK;
+}
+
+int fg_world_set_fused_integrate(fg_world *w, int fused)
+{
+    if (!w) return FG_E_INVALID;
+    ((World *)w)->fused_integrate = fused != 0;
+    return FG_OK;
+}
+
+int fg_world_set_sort_digit_bits(fg_world *w, uint32_t bits)
+{
+    if (!w || bits < 1 || bits > 8) return FG_E_INVALID;
+    ((World *)w)->digit_bits = bits;
+    return FG_OK;
+}
+
+int fg_world_set_graphs(fg_world *w, int on)
+{
+    if (!w) return FG_E_INVALID;
+    ((World *)w)->use_graphs = on != 0;
+    return FG_OK;
+}
+
+uint32_t fg_world_launches_per_step(const fg_world *w)
+{
+    if (!w) return 0;
+    return ((World *)w)->launches_per_step();
+}
+
+int fg_memcpy_d2h(void *dst, const void *src, size_t bytes)
+{
+    if (!bytes) return FG_OK;
+    CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    return FG_OK;
+}
+
+int fg_memcpy_h2d(void *dst, const void *src, size_t bytes)
+{
+    if (!bytes) return FG_OK;
+    CK(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+    return FG_OK;
+}
+
+int fg_device_synchronize(void)
+{
+    CK(cudaDeviceSynchronize());
+    return FG_OK;
+}
+
+int fg_world_stage_profile(fg_world *w, size_t flush_bytes, float stage_ms[8])
+{
+    if (!w || !stage_ms) return FG_E_INVALID;
+    return ((World *)w)->stage_profile(flush_bytes, stage_ms);
+}
+
+int fg_world_timed_steps(fg_world *w, uint32_t nsteps, size_t flush_bytes, float *ms)
+{
+    if (!w || (!ms && nsteps)) return FG_E_INVALID;
+    return ((World *)w)->timed_steps(nsteps, flush_bytes, ms);
+}
+
+int fg_world_e2e_steps(fg_world *w, uint32_t nsteps, const float *host_pos4, const float *host_vel4,
+                       float *out_pos4, float *out_vel4, float *ms)
+{
+    if (!w || !host_pos4 || !host_vel4 || !out_pos4 || !out_vel4 || (!ms && nsteps)) return FG_E_INVALID;
+    return ((World *)w)->e2e_steps(nsteps, host_pos4, host_vel4, out_pos4, out_vel4, ms);
+}
+
+void *fg_host_alloc(size_t bytes)
+{
+    void *p = nullptr;
+    if (cudaMallocHost(&p, bytes ? bytes : 16) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+int fg_host_free(void *p)
+{
+    if (!p) return FG_OK;
+    CK(cudaFreeHost(p));
+    return FG_OK;
+}
+
+int fg_set_device(int device)
+{
+    CK(cudaSetDevice(device));
+    return FG_OK;
+}
+
+int fg_probe_fp32_peak(float *tflops)
+{
+    if (!tflops) return FG_E_INVALID;
+    return fg::probe_fp32(tflops);
+}
+
+const char *fg_last_error(void) { return fg::g_err.c_str(); }
+
+const char *fg_version(void) { return "fluidgrid_gb300 0.1 sm_103a"; }
+
+} /* extern "C" */

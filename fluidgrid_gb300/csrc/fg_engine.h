@@ -1,0 +1,77 @@
+/* World engine internals (host side). */
+#ifndef FG_ENGINE_H
+#define FG_ENGINE_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <vector>
+#include "fg_types.h"
+#include "fg_kernels.h"
+
+struct fg_scene_desc;
+
+namespace fg {
+
+void set_error(const char *what, cudaError_t e);
+void set_error_msg(const char *what);
+void fill_scene(FgScene &S, const fg_scene_desc &d);
+int validate(const fg_scene_desc &d);
+
+struct World {
+    /* layout */
+    uint32_t nscenes = 0, n = 0, total_buckets = 0, nspheres = 0, nbodies = 0, total_rb_buckets = 0;
+    uint32_t nwork = 0, nwork_sph = 0;
+    uint32_t key_bits = 0, rb_key_bits = 0, digit_bits = 8;
+    bool single = true;
+    bool any_rb_rb = false;
+    std::vector<FgScene> scenes_h;
+    FgScene *scenes_d = nullptr;
+    FgWork *work_d = nullptr, *work_sph_d = nullptr;
+    /* fluid */
+    float4 *pos = nullptr, *vel = nullptr, *spos = nullptr, *svel = nullptr;
+    float2 *dp = nullptr;
+    uint32_t *keys_u = nullptr, *keys = nullptr, *ids = nullptr, *start = nullptr, *end = nullptr;
+    RadixScratch rs{nullptr, nullptr, nullptr};
+    /* rigid */
+    float4 *rb_local = nullptr, *rb_world = nullptr, *rb_spos = nullptr, *rb_force = nullptr, *rb_torque = nullptr;
+    uint32_t *rb_keys_u = nullptr, *rb_keys = nullptr, *rb_ids = nullptr, *rb_start = nullptr, *rb_end = nullptr;
+    int *aabb = nullptr;
+    FgD4 *bx = nullptr, *bv = nullptr, *bq = nullptr, *bL = nullptr, *bfs = nullptr, *bts = nullptr;
+    float4 *bxf = nullptr, *bvf = nullptr, *bqf = nullptr;
+    double *bmass = nullptr, *binv = nullptr;
+    uint32_t *body_scene = nullptr, *body_first = nullptr, *body_count = nullptr;
+    uint32_t *status_d = nullptr;
+    /* execution */
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    uint32_t stages = 255;
+    bool fused_integrate = true;
+    bool use_graphs = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    uint32_t graph_stages = 0, graph_digits = 0;
+    bool graph_fused = true;
+    std::vector<void *> allocs;
+    size_t device_bytes = 0;
+
+    ~World();
+    int alloc(void **p, size_t bytes);
+    int create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st);
+    Launch fluid_launch() const;
+    Launch sphere_launch() const;
+    uint32_t enqueue_step(cudaEvent_t *stage_events = nullptr);
+    uint32_t *flush_buf = nullptr;
+    size_t flush_bytes = 0;
+    int step(uint32_t nsteps);
+    uint32_t launches_per_step();
+    int check();
+    int sync();
+    int ensure_flush(size_t bytes);
+    int stage_profile(size_t flush_bytes, float *ms);
+    int timed_steps(uint32_t nsteps, size_t flush_bytes, float *ms);
+    int e2e_steps(uint32_t nsteps, const float *hp, const float *hv, float *op, float *ov, float *ms);
+};
+
+} // namespace fg
+
+#endif

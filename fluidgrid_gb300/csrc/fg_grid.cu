@@ -1,0 +1,401 @@
+/* Hash-grid build on GB300: particle hash, stable key/index radix sort, cell
+ * start/end ranges with the sorted gather of position and velocity.
+ *
+ * Follows the reference's grid build (GPU_Kernels/K_HashGrid.cu:26-197 and the
+ * thrust/CUDPP key-value sorts, K_FluidSim.cu:685-691,
+ * RigidBodySimulator.cpp:195-196) with identical results: keys bit-exact,
+ * ascending key order with ties in particle-index order, same start/end
+ * entries.  All kernels stream coalesced 16-byte loads; the sort is a
+ * reduce-then-scan LSD radix sort whose CTAs never wait on one another. */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <algorithm>
+#include "fg_device.cuh"
+#include "fg_kernels.h"
+
+namespace fg {
+
+int sm_count()
+{
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+            sms = 152;
+    }
+    return sms;
+}
+
+uint32_t grid_for(uint32_t nwork, int ctas_per_sm)
+{
+    uint32_t cap = (uint32_t)sm_count() * (uint32_t)ctas_per_sm;
+    return std::max(1u, std::min(nwork, cap));
+}
+
+/* ------------------------------------------------------------- hashing */
+
+/* CalcHashKeyK (K_HashGrid.cu:26-38): key = bucket_base + HashKeyD(pos),
+ * id = particle index. */
+__global__ void __launch_bounds__(FG_CHUNK) k_hash(const FgWork *__restrict__ work, uint32_t nwork, uint32_t n_single,
+                                                  const FgScene *__restrict__ table,
+                                                  const __grid_constant__ FgScene single,
+                                                  const float4 *__restrict__ pos, uint32_t *__restrict__ keys,
+                                                  uint32_t *__restrict__ ids)
+{
+    for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+        FgWork it = fg_work(work, w, n_single);
+        const FgScene *S = fg_scene(table, &single, it.scene);
+        if (threadIdx.x < it.count) {
+            uint32_t i = it.first + threadIdx.x;
+            float4 p = __ldg(pos + i);
+            keys[i] = S->bucket_base + fg_hash(p.x, p.y, p.z, S->cell, S->nb, S->nb_mask);
+            if (ids) ids[i] = i;
+        }
+    }
+}
+
+void launch_hash(const Launch &L, const float4 *pos, uint32_t *keys, uint32_t *ids)
+{
+    if (!L.nwork) return;
+    k_hash<<<grid_for(L.nwork, 16), FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, pos, keys,
+                                                             ids);
+}
+
+/* CalcHashKeyWithOffsetK (K_HashGrid.cu:43-63): world = conj(q)*p*q + cm of
+ * the sphere's body (w = body index), key of the world position in the
+ * rigid grid.  Optionally grows the per-scene AABB of sphere centres (six
+ * ordered ints: min xyz, max xyz). */
+__global__ void __launch_bounds__(FG_CHUNK) k_hash_offset(const FgWork *__restrict__ work, uint32_t nwork,
+                                                         uint32_t n_single, const FgScene *__restrict__ table,
+                                                         const __grid_constant__ FgScene single,
+                                                         const float4 *__restrict__ local,
+                                                         const float4 *__restrict__ cm,
+                                                         const float4 *__restrict__ q, float4 *__restrict__ world,
+                                                         uint32_t *__restrict__ keys, uint32_t *__restrict__ ids,
+                                                         int *__restrict__ aabb)
+{
+    for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+        FgWork it = fg_work(work, w, n_single);
+        const FgScene *S = fg_scene(table, &single, it.scene);
+        bool ok = threadIdx.x < it.count;
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (ok) {
+            uint32_t i = it.first + threadIdx.x;
+            float4 p = __ldg(local + i);
+            int b = (int)p.w;
+            float4 t = fg_qtransform_rn(p, __ldg(q + b));
+            float4 o = __ldg(cm + b);
+            a.x = __fadd_rn(t.x, o.x);
+            a.y = __fadd_rn(t.y, o.y);
+            a.z = __fadd_rn(t.z, o.z);
+            a.w = p.w;
+            world[i] = a;
+            keys[i] = S->rb_bucket_base + fg_hash(a.x, a.y, a.z, S->rb_cell, S->rb_nb, S->rb_nb_mask);
+            if (ids) ids[i] = i;
+        }
+        if (aabb) {
+            /* warp-reduce then one atomic per warp per bound */
+            float mn[3] = {ok ? a.x : 3.0e38f, ok ? a.y : 3.0e38f, ok ? a.z : 3.0e38f};
+            float mx[3] = {ok ? a.x : -3.0e38f, ok ? a.y : -3.0e38f, ok ? a.z : -3.0e38f};
+#pragma unroll
+            for (int d = 0; d < 3; d++)
+#pragma unroll
+                for (int o = 16; o; o >>= 1) {
+                    mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+                    mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+                }
+            if ((threadIdx.x & 31) == 0 && (threadIdx.x >> 5) * 32 < it.count) {
+                int *bx = aabb + 6 * it.scene;
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    atomicMin(bx + d, fg_float_ord(mn[d]));
+                    atomicMax(bx + 3 + d, fg_float_ord(mx[d]));
+                }
+            }
+        }
+    }
+}
+
+void launch_hash_with_offset(const Launch &L, const float4 *local, const float4 *cm, const float4 *q, float4 *world,
+                             uint32_t *keys, uint32_t *ids, int *aabb)
+{
+    if (!L.nwork) return;
+    k_hash_offset<<<grid_for(L.nwork, 16), FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, local,
+                                                                    cm, q, world, keys, ids, aabb);
+}
+
+/* ----------------------------------------------------------- radix sort
+ * LSD radix sort, up to 8 bits per pass, tiles of RS_TILE keys:
+ *   upsweep   per-tile digit counts          hist[d * T + t]
+ *   scan      per digit, exclusive over tiles  (one CTA per digit) + totals
+ *   downsweep stable in-tile ranking (warp match_any), shared-memory
+ *             staging in digit order, coalesced scatter.
+ * Ranks within a tile follow particle order (warp w holds keys
+ * [w*512, w*512+512) of the tile, item k of lane l is key w*512 + 32k + l and
+ * items are ranked k-major, lane-minor), so each pass is stable. */
+
+#define RS_THREADS 256
+#define RS_ITEMS 16
+#define RS_TILE (RS_THREADS * RS_ITEMS)
+#define RS_RADIX 256
+#define RS_WARPS (RS_THREADS / 32)
+
+size_t radix_hist_words(uint32_t n)
+{
+    size_t tiles = ((size_t)n + RS_TILE - 1) / RS_TILE;
+    return (size_t)RS_RADIX * std::max<size_t>(tiles, 1) + RS_RADIX;
+}
+
+int radix_passes(uint32_t bits, uint32_t digit_bits)
+{
+    if (digit_bits < 1) digit_bits = 1;
+    if (digit_bits > 8) digit_bits = 8;
+    return (int)((bits + digit_bits - 1) / digit_bits);
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const uint32_t *__restrict__ keys, uint32_t n,
+                                                          uint32_t shift, uint32_t mask, uint32_t *__restrict__ hist,
+                                                          uint32_t T)
+{
+    __shared__ uint32_t cnt[RS_RADIX];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    size_t base = (size_t)blockIdx.x * RS_TILE;
+#pragma unroll 4
+    for (int k = 0; k < RS_ITEMS; k++) {
+        size_t i = base + (size_t)k * RS_THREADS + threadIdx.x;
+        if (i < n) atomicAdd(&cnt[(__ldg(keys + i) >> shift) & mask], 1u);
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * T + blockIdx.x] = cnt[threadIdx.x];
+}
+
+/* block-wide exclusive scan of one value per thread (RS_THREADS threads) */
+__device__ __forceinline__ uint32_t rs_block_excl(uint32_t v, uint32_t *s_warp, uint32_t &total)
+{
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) s_warp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t t = lane < RS_WARPS ? s_warp[lane] : 0;
+        uint32_t u = t;
+#pragma unroll
+        for (int o = 1; o < RS_WARPS; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, u, o);
+            if (lane >= (uint32_t)o) u += y;
+        }
+        if (lane < RS_WARPS) s_warp[lane] = u - t;
+        if (lane == RS_WARPS - 1) s_warp[RS_WARPS] = u;
+    }
+    __syncthreads();
+    uint32_t r = x - v + s_warp[wid];
+    total = s_warp[RS_WARPS];
+    __syncthreads();
+    return r;
+}
+
+/* One CTA per digit: exclusive scan of hist[d*T .. d*T+T) in place. */
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scan(uint32_t *__restrict__ hist, uint32_t T,
+                                                       uint32_t *__restrict__ totals)
+{
+    __shared__ uint32_t s_warp[RS_WARPS + 1];
+    uint32_t *h = hist + (size_t)blockIdx.x * T;
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < T; base += RS_THREADS) {
+        uint32_t i = base + threadIdx.x;
+        uint32_t v = i < T ? h[i] : 0;
+        uint32_t tot;
+        uint32_t e = rs_block_excl(v, s_warp, tot);
+        if (i < T) h[i] = e + carry;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) totals[blockIdx.x] = carry;
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const uint32_t *__restrict__ kin,
+                                                            const uint32_t *__restrict__ vin,
+                                                            uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
+                                                            uint32_t n, uint32_t shift, uint32_t mask,
+                                                            const uint32_t *__restrict__ hist,
+                                                            const uint32_t *__restrict__ totals, uint32_t T)
+{
+    __shared__ uint32_t s_keys[RS_TILE];
+    __shared__ uint32_t s_vals[RS_TILE];
+    __shared__ uint32_t s_whist[RS_WARPS][RS_RADIX];
+    __shared__ uint32_t s_goff[RS_RADIX];
+    __shared__ uint32_t s_tstart[RS_RADIX];
+    __shared__ uint32_t s_warp[RS_WARPS + 1];
+
+    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const size_t base = (size_t)blockIdx.x * RS_TILE;
+
+    /* global offset of each digit for this tile */
+    {
+        uint32_t tot;
+        uint32_t gb = rs_block_excl(totals[tid], s_warp, tot);
+        s_goff[tid] = gb + hist[(size_t)tid * T + blockIdx.x];
+    }
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) s_whist[w][tid] = 0;
+    __syncthreads();
+
+    uint32_t key[RS_ITEMS], val[RS_ITEMS], rank[RS_ITEMS];
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < RS_ITEMS; k++) {
+        size_t i = base + (size_t)wid * (32 * RS_ITEMS) + (size_t)k * 32 + lane;
+        bool valid = i < n;
+        key[k] = valid ? __ldg(kin + i) : 0xffffffffu;
+        val[k] = valid ? (vin ? __ldg(vin + i) : (uint32_t)i) : 0u;
+        uint32_t active = __ballot_sync(0xffffffffu, valid);
+        uint32_t r = 0;
+        if (valid) {
+            uint32_t d = (key[k] >> shift) & mask;
+            uint32_t peers = __match_any_sync(active, d);
+            uint32_t leader = __ffs(peers) - 1;
+            uint32_t b = 0;
+            if (lane == leader) {
+                b = s_whist[wid][d];
+                s_whist[wid][d] = b + __popc(peers);
+            }
+            b = __shfl_sync(active, b, leader);
+            r = b + __popc(peers & lt);
+        }
+        rank[k] = r;
+        __syncwarp();
+    }
+    __syncthreads();
+    /* per digit: exclusive over warps, tile count */
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) {
+        uint32_t c = s_whist[w][tid];
+        s_whist[w][tid] = run;
+        run += c;
+    }
+    {
+        uint32_t tot;
+        uint32_t ts = rs_block_excl(run, s_warp, tot);
+        s_tstart[tid] = ts;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < RS_ITEMS; k++) {
+        size_t i = base + (size_t)wid * (32 * RS_ITEMS) + (size_t)k * 32 + lane;
+        if (i < n) {
+            uint32_t d = (key[k] >> shift) & mask;
+            uint32_t p = s_tstart[d] + s_whist[wid][d] + rank[k];
+            s_keys[p] = key[k];
+            s_vals[p] = val[k];
+        }
+    }
+    __syncthreads();
+    uint32_t tile_n = (n - base) < (size_t)RS_TILE ? (uint32_t)(n - base) : (uint32_t)RS_TILE;
+    for (uint32_t i = tid; i < tile_n; i += RS_THREADS) {
+        uint32_t kk = s_keys[i];
+        uint32_t d = (kk >> shift) & mask;
+        uint32_t g = s_goff[d] + (i - s_tstart[d]);
+        kout[g] = kk;
+        vout[g] = s_vals[i];
+    }
+}
+
+__global__ void k_iota_copy(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
+                            uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint32_t n)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        kout[i] = kin[i];
+        vout[i] = vin ? vin[i] : i;
+    }
+}
+
+void radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out, uint32_t n,
+                uint32_t bits, uint32_t digit_bits, const RadixScratch &s, cudaStream_t st)
+{
+    if (n == 0) return;
+    if (digit_bits < 1) digit_bits = 1;
+    if (digit_bits > 8) digit_bits = 8;
+    const int P = radix_passes(bits, digit_bits);
+    if (P == 0) {
+        if (keys_in != keys_out || vals_in != vals_out || !vals_in)
+            k_iota_copy<<<grid_for((n + 255) / 256, 8), 256, 0, st>>>(keys_in, vals_in, keys_out, vals_out, n);
+        return;
+    }
+    const uint32_t T = (n + RS_TILE - 1) / RS_TILE;
+    uint32_t *totals = s.hist + (size_t)RS_RADIX * T;
+    const bool inplace = (keys_in == keys_out);
+    /* choose the first destination so the last pass lands in *_out */
+    const uint32_t *kin = keys_in;
+    const uint32_t *vin = vals_in;
+    bool to_out = (P % 2 == 1) && !inplace;
+    for (int p = 0; p < P; p++) {
+        uint32_t shift = (uint32_t)p * digit_bits;
+        uint32_t b = std::min(digit_bits, bits - shift);
+        uint32_t mask = (1u << b) - 1u;
+        uint32_t *ko = to_out ? keys_out : s.keys_alt;
+        uint32_t *vo = to_out ? vals_out : s.vals_alt;
+        k_rs_upsweep<<<T, RS_THREADS, 0, st>>>(kin, n, shift, mask, s.hist, T);
+        k_rs_scan<<<RS_RADIX, RS_THREADS, 0, st>>>(s.hist, T, totals);
+        k_rs_downsweep<<<T, RS_THREADS, 0, st>>>(kin, vin, ko, vo, n, shift, mask, s.hist, totals, T);
+        kin = ko;
+        vin = vo;
+        to_out = !to_out;
+    }
+    if (kin != keys_out) {
+        cudaMemcpyAsync(keys_out, kin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(vals_out, vin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+    }
+}
+
+/* ------------------------------------------------------ ranges + reorder
+ * FindCellOffsetOrderinPosVelK / FindCellOffsetOrderingPosK
+ * (K_HashGrid.cu:70-197): start[key] at the first index of each key run,
+ * end[previous key] = that index, end[last key] = n; sorted gather of
+ * position (and velocity). */
+__global__ void __launch_bounds__(256) k_cell_ranges(const uint32_t *__restrict__ keys,
+                                                    const uint32_t *__restrict__ ids,
+                                                    const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                                                    uint32_t *__restrict__ start, uint32_t *__restrict__ end,
+                                                    float4 *__restrict__ spos, float4 *__restrict__ svel, uint32_t n)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t k = __ldg(keys + i);
+        uint32_t prev = i > 0 ? __ldg(keys + i - 1) : k;
+        if (i == 0 || k != prev) {
+            start[k] = i;
+            if (i > 0) end[prev] = i;
+        }
+        if (i == n - 1) end[k] = n;
+        uint32_t id = __ldg(ids + i);
+        spos[i] = __ldg(pos + id);
+        if (vel) svel[i] = __ldg(vel + id);
+    }
+}
+
+void launch_cell_ranges(const uint32_t *keys, const uint32_t *ids, const float4 *pos, const float4 *vel,
+                        uint32_t *start, uint32_t *end, float4 *spos, float4 *svel, uint32_t n, cudaStream_t st)
+{
+    if (!n) return;
+    k_cell_ranges<<<grid_for((n + 255) / 256, 8), 256, 0, st>>>(keys, ids, pos, vel, start, end, spos, svel, n);
+}
+
+__global__ void k_fill(uint32_t *buf, size_t words, uint32_t v)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x)
+        buf[i] = v;
+}
+
+void launch_fill(uint32_t *buf, size_t words, uint32_t v, cudaStream_t s)
+{
+    if (!words) return;
+    k_fill<<<grid_for((uint32_t)std::min<size_t>((words + 255) / 256, 1u << 30), 8), 256, 0, s>>>(buf, words, v);
+}
+
+} // namespace fg

@@ -1,0 +1,118 @@
+/* Host-side launch wrappers of the GB300 SPH kernels (internal). */
+#ifndef FG_KERNELS_H
+#define FG_KERNELS_H
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+#include "fg_types.h"
+
+namespace fg {
+
+/* Launch geometry: work items of FG_CHUNK particles; grids are sized in
+ * multiples of the SM count (persistent grid-stride loops). */
+struct Launch {
+    const FgScene *table;  /* device scene table, or nullptr for one scene */
+    const FgScene *single; /* host copy used when table == nullptr (passed by value) */
+    const FgWork *work;    /* device work table, or nullptr (single scene) */
+    uint32_t nwork;        /* work items */
+    uint32_t n;            /* particles (single-scene mode) */
+    cudaStream_t stream;
+};
+
+int sm_count();
+uint32_t grid_for(uint32_t nwork, int ctas_per_sm);
+
+/* ---- grid build (fg_grid.cu) ---- */
+void launch_hash(const Launch &L, const float4 *pos, uint32_t *keys, uint32_t *ids);
+void launch_hash_with_offset(const Launch &L, const float4 *local, const float4 *cm, const float4 *q,
+                             float4 *world, uint32_t *keys, uint32_t *ids, int *aabb /* 6 ints per scene or null */);
+
+struct RadixScratch {
+    uint32_t *keys_alt;
+    uint32_t *vals_alt;
+    uint32_t *hist; /* >= radix_hist_words(n) words */
+};
+size_t radix_hist_words(uint32_t n);
+int radix_passes(uint32_t bits, uint32_t digit_bits);
+/* Stable ascending sort of (key, value) by the low `bits` bits of the key.
+ * vals_in == nullptr means values 0..n-1.  keys_out/vals_out may alias
+ * keys_in/vals_in (in-place). */
+void radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
+                uint32_t n, uint32_t bits, uint32_t digit_bits, const RadixScratch &s, cudaStream_t st);
+
+/* start[] must be pre-filled with 0xffffffff over the bucket range. */
+void launch_cell_ranges(const uint32_t *keys, const uint32_t *ids, const float4 *pos, const float4 *vel,
+                        uint32_t *start, uint32_t *end, float4 *spos, float4 *svel, uint32_t n, cudaStream_t st);
+
+/* ---- SPH (fg_sph.cu) ---- */
+void launch_density(const Launch &L, const float4 *spos, const uint32_t *start, const uint32_t *end, float2 *dp,
+                    float gas_override, float rest_override, float mass_override, int use_override);
+
+struct RigidGrid {
+    const float4 *spos;     /* sorted sphere positions, w = body index */
+    const uint32_t *start;  /* rigid bucket table */
+    const uint32_t *end;
+    const float4 *body_vel; /* per-body velocity (float); null = static grid */
+    const int *aabb;        /* per scene ordered-int AABB of sphere centres, or null */
+    int own_geometry;       /* 1: bucket count below (bucket base 0); 0: the scene's rigid grid */
+    uint32_t nb, mask;
+};
+
+struct ForceOut {
+    float4 *vel;  /* unsorted velocity, written at ids[i] */
+    float4 *pos;  /* unsorted position; non-null = fused integration */
+};
+
+void launch_forces(const Launch &L, const float4 *spos, const float4 *svel, const float2 *dp, const uint32_t *start,
+                   const uint32_t *end, const uint32_t *ids, ForceOut out, const RigidGrid *rigid,
+                   const RigidGrid *statics, float mass_override, float visc_override, int use_override);
+
+void launch_integrate(const Launch &L, float4 *pos, const float4 *vel);
+
+/* ---- rigid bodies (fg_rigid.cu) ---- */
+void launch_rb_from_fluid(const Launch &Lrb, const float4 *rb_spos, const uint32_t *rb_ids, const float4 *body_vel,
+                          const float4 *body_cm, const float4 *fl_spos, const float4 *fl_svel,
+                          const uint32_t *fl_start, const uint32_t *fl_end, float4 *force, float4 *torque,
+                          int add);
+
+/* add = 1: accumulate xyz into force/torque at the sphere's unsorted index;
+ * add = 0: write (w = body index).  statics: optional static sphere grid
+ * (numSRB > 0 in the reference). */
+void launch_rb_from_rb(const Launch &Lrb, const float4 *rb_spos, const uint32_t *rb_ids, const float4 *body_vel,
+                       const float4 *body_cm, const uint32_t *rb_start, const uint32_t *rb_end, float4 *force,
+                       float4 *torque, const RigidGrid *statics, int add);
+
+struct BodyState {
+    FgD4 *x, *v, *q, *L;  /* FP64 state per body */
+    const double *inv_inertia; /* 9 per body, row-major */
+    const double *mass;
+    float4 *x_f, *v_f, *q_f; /* FP32 mirrors read by the contact kernels */
+    FgD4 *force_sum, *torque_sum; /* FP64 per-body sums (diagnostic output) */
+};
+
+/* Per body: FP64 sum of its spheres' force/torque (unsorted, body-contiguous
+ * sphere ranges) followed by the FP64 body integrator. */
+void launch_body_update(const FgScene *table, const FgScene *single, const uint32_t *body_scene,
+                        const uint32_t *body_first, const uint32_t *body_count, uint32_t nbodies,
+                        const float4 *force, const float4 *torque, BodyState st, int integrate, cudaStream_t s);
+
+/* FP32 body integrator with the reference's arithmetic (IntegrateRBK). */
+void launch_integrate_rb_f32(float4 *x, const float *mass, float4 *v, const float4 *f, uint32_t nrb, float dt,
+                             float4 ext, float3 vmin, float3 vmax, float4 *L, const float4 *t,
+                             const float4 *inertia, float4 *q, const float4 *inv, float vlimit, cudaStream_t s);
+
+/* reduction helpers with the reference's data flow */
+void launch_copy_rb_data_to_particle(uint32_t *key, uint32_t *idx, const float4 *force, uint32_t n, cudaStream_t s);
+void launch_reorder_force_torque(float4 *fo, float4 *to, const float4 *fi, const float4 *ti, const uint32_t *order,
+                                 uint32_t n, cudaStream_t s);
+void launch_segmented_sum(const float4 *in, const uint32_t *flags, float4 *out, uint32_t n, cudaStream_t s);
+void launch_add_force_torque(const float4 *sum_f, const float4 *sum_t, const float4 *ordered_f, float4 *out_f,
+                             float4 *out_t, const int *offsets, uint32_t nrb, cudaStream_t s);
+
+/* L2 flush helper used by the benchmark */
+void launch_fill(uint32_t *buf, size_t words, uint32_t v, cudaStream_t s);
+
+} // namespace fg
+
+#endif

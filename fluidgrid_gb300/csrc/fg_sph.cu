@@ -1,0 +1,292 @@
+/* SPH density, forces and integration on GB300.
+ *
+ * Semantics follow GPU_Kernels/K_FluidSim.cu:
+ *   density   CalculateMassDensityK + ProcessMassDensityGridD (:46-79, :210-254)
+ *   forces    SPHCalculateForcesK / SPHCalculateForcesWithSRBK with
+ *             CalculateFluidInternalForcesD, SPHCalculatePressureForceD,
+ *             SPHCalculateViscosityForceD (:85-205, :260-413), walls from
+ *             K_Boundaries_Walls.cu, rigid contact ProcessCollisionForcesD
+ *             (K_DeviceFunctions.cu:32-159)
+ *   integrate SPHIntegrateK (:418-438)
+ * The 27 neighbour buckets are visited exactly as the reference visits them
+ * (z-y-x order, same hashed buckets, a bucket reached twice is summed twice);
+ * bucket indices are bit-exact.  Pair arithmetic is reorganised for the
+ * GPU: squared-distance tests, rsqrt/rcp instead of divides, compensated
+ * (Kahan) density sums; the results agree with the reference arithmetic to
+ * the tolerances the parity tests state.
+ *
+ * One thread per particle in sorted order: neighbouring lanes share cells,
+ * so neighbour loads broadcast from L1 and sorted float4 loads coalesce. */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "fg_device.cuh"
+#include "fg_kernels.h"
+
+namespace fg {
+
+/* Kahan-compensated accumulator */
+struct Kahan {
+    float s, c;
+    __device__ __forceinline__ void add(float x)
+    {
+        float y = x - c;
+        float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
+__global__ void __launch_bounds__(FG_CHUNK) k_density(const FgWork *__restrict__ work, uint32_t nwork,
+                                                     uint32_t n_single, const FgScene *__restrict__ table,
+                                                     const __grid_constant__ FgScene single,
+                                                     const float4 *__restrict__ spos,
+                                                     const uint32_t *__restrict__ start,
+                                                     const uint32_t *__restrict__ end, float2 *__restrict__ dp,
+                                                     float gas_o, float rest_o, float mass_o, int use_o)
+{
+    for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+        FgWork it = fg_work(work, w, n_single);
+        if (threadIdx.x >= it.count) continue;
+        const FgScene *S = fg_scene(table, &single, it.scene);
+        const uint32_t i = it.first + threadIdx.x;
+        const float4 p = spos[i];
+        if (!(p.w > 0.0f)) continue; /* inactive: density not written */
+        const float scale = S->scale, h2 = S->h2;
+        const uint32_t nb = S->nb, mask = S->nb_mask, bb = S->bucket_base;
+        uint32_t hx[3], hy[3], hz[3];
+        fg_neighbour_hashes(p.x, p.y, p.z, S->cell, hx, hy, hz);
+        const float px = p.x * scale, py = p.y * scale, pz = p.z * scale;
+        Kahan acc = {0.f, 0.f};
+#pragma unroll 1
+        for (int z = 0; z < 3; z++)
+#pragma unroll 1
+            for (int y = 0; y < 3; y++)
+#pragma unroll 1
+                for (int x = 0; x < 3; x++) {
+                    const uint32_t b = bb + fg_bucket(hx[x], hy[y], hz[z], nb, mask);
+                    const uint32_t st = __ldg(start + b);
+                    if (st == FG_EMPTY) continue;
+                    const uint32_t en = __ldg(end + b);
+                    for (uint32_t j = st; j < en; j++) {
+                        const float4 q = __ldg(spos + j);
+                        const float dx = px - q.x * scale, dy = py - q.y * scale, dz = pz - q.z * scale;
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        if (r2 < h2) {
+                            const float t = h2 - r2;
+                            acc.add(t * t * t);
+                        }
+                    }
+                }
+        const float mass = use_o ? mass_o : S->mass;
+        const float gas = use_o ? gas_o : S->gas;
+        const float rest = use_o ? rest_o : S->rest;
+        const float rho = (mass * S->kpoly6) * acc.s;
+        dp[i] = make_float2(fmaxf(1.0f, rho), gas * (rho - rest));
+    }
+}
+
+void launch_density(const Launch &L, const float4 *spos, const uint32_t *start, const uint32_t *end, float2 *dp,
+                    float gas_o, float rest_o, float mass_o, int use_o)
+{
+    if (!L.nwork) return;
+    k_density<<<grid_for(L.nwork, 16), FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos,
+                                                                start, end, dp, gas_o, rest_o, mass_o, use_o);
+}
+
+/* Rigid-sphere contact of one fluid particle against a rigid grid
+ * (ProcessCollisionForcesD with the per-body velocity of w, eps from the
+ * scene).  Skipped when the particle is outside the scene's sphere AABB
+ * grown by the contact distance: there every candidate is out of range, so
+ * the sum is exactly zero as in the reference. */
+__device__ __forceinline__ float3 fg_fluid_rigid_contact(const FgScene *S, uint32_t scene, float4 p, float4 v,
+                                                         const RigidGrid &G, bool dynamic)
+{
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+    const float mind = S->fluid_radius + S->rb_radius + S->fluid_eps;
+    if (G.aabb) {
+        const int *bx = G.aabb + 6 * scene;
+        if (p.x < fg_ord_float(bx[0]) - mind || p.y < fg_ord_float(bx[1]) - mind ||
+            p.z < fg_ord_float(bx[2]) - mind || p.x > fg_ord_float(bx[3]) + mind ||
+            p.y > fg_ord_float(bx[4]) + mind || p.z > fg_ord_float(bx[5]) + mind)
+            return acc;
+    }
+    const float3 P = make_float3(p.x, p.y, p.z);
+    const float3 V = make_float3(v.x, v.y, v.z);
+    const int rx = S->f2r_rel[0], ry = S->f2r_rel[1], rz = S->f2r_rel[2];
+    for (int z = -rz; z <= rz; z++) {
+        const uint32_t hz = fg_axis_hash_rel(p.z, S->rb_cell[2], z, FG_PZ);
+        for (int y = -ry; y <= ry; y++) {
+            const uint32_t hy = fg_axis_hash_rel(p.y, S->rb_cell[1], y, FG_PY);
+            for (int x = -rx; x <= rx; x++) {
+                const uint32_t hx = fg_axis_hash_rel(p.x, S->rb_cell[0], x, FG_PX);
+                const uint32_t b = G.own_geometry ? fg_bucket(hx, hy, hz, G.nb, G.mask)
+                                                  : S->rb_bucket_base + fg_bucket(hx, hy, hz, S->rb_nb, S->rb_nb_mask);
+                const uint32_t st = __ldg(G.start + b);
+                if (st == FG_EMPTY) continue;
+                const uint32_t en = __ldg(G.end + b);
+                for (uint32_t j = st; j < en; j++) {
+                    const float4 q = __ldg(G.spos + j);
+                    const float4 vq = dynamic ? __ldg(G.body_vel + (int)q.w) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    fg_contact(acc, P, V, q, vq, mind, S->ck, S->ckd);
+                }
+            }
+        }
+    }
+    return acc;
+}
+
+struct RigidArgs {
+    RigidGrid dyn;
+    RigidGrid sta;
+    int use_dyn, use_sta;
+};
+
+__global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ work, uint32_t nwork,
+                                                    uint32_t n_single, const FgScene *__restrict__ table,
+                                                    const __grid_constant__ FgScene single,
+                                                    const float4 *__restrict__ spos, const float4 *__restrict__ svel,
+                                                    const float2 *__restrict__ dp,
+                                                    const uint32_t *__restrict__ start,
+                                                    const uint32_t *__restrict__ end,
+                                                    const uint32_t *__restrict__ ids, float4 *__restrict__ vel_out,
+                                                    float4 *__restrict__ pos_out,
+                                                    const __grid_constant__ RigidArgs R, float mass_o, float visc_o,
+                                                    int use_o)
+{
+    for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+        FgWork it = fg_work(work, w, n_single);
+        if (threadIdx.x >= it.count) continue;
+        const FgScene *S = fg_scene(table, &single, it.scene);
+        const uint32_t i = it.first + threadIdx.x;
+        const float4 p = spos[i];
+        const float4 v = svel[i];
+        float3 F = make_float3(0.f, 0.f, 0.f);
+        if (p.w > 0.0f) {
+            const float scale = S->scale, h = S->h, h2 = S->h2;
+            const uint32_t nb = S->nb, mask = S->nb_mask, bb = S->bucket_base;
+            const float mass = use_o ? mass_o : S->mass;
+            const float visc = use_o ? visc_o : S->visc;
+            const float2 di = dp[i];
+            const float kspiky = S->kspiky, kv = S->kvisc * visc;
+            uint32_t hx[3], hy[3], hz[3];
+            fg_neighbour_hashes(p.x, p.y, p.z, S->cell, hx, hy, hz);
+            const float px = p.x * scale, py = p.y * scale, pz = p.z * scale;
+            float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll 1
+            for (int z = 0; z < 3; z++)
+#pragma unroll 1
+                for (int y = 0; y < 3; y++)
+#pragma unroll 1
+                    for (int x = 0; x < 3; x++) {
+                        const uint32_t b = bb + fg_bucket(hx[x], hy[y], hz[z], nb, mask);
+                        const uint32_t st = __ldg(start + b);
+                        if (st == FG_EMPTY) continue;
+                        const uint32_t en = __ldg(end + b);
+                        for (uint32_t j = st; j < en; j++) {
+                            if (j == i) continue;
+                            const float4 q = __ldg(spos + j);
+                            const float dx = px - q.x * scale, dy = py - q.y * scale, dz = pz - q.z * scale;
+                            const float r2 = dx * dx + dy * dy + dz * dz;
+                            if (r2 <= h2) {
+                                const float4 vj = __ldg(svel + j);
+                                const float2 dj = __ldg(dp + j);
+                                const float il = rsqrtf(r2);
+                                const float l = r2 * il;
+                                const float hl = h - l;
+                                const float irr = __frcp_rn(di.x * dj.x);
+                                /* pressure: -(d/l) kSpiky (h-l)^2 (Pi+Pj)/(rho_i rho_j) */
+                                const float cp = -(kspiky * hl * hl) * ((di.y + dj.y) * irr) * il;
+                                /* viscosity: (vj-vi)/(rho_i rho_j) kVisc (h-l) mu */
+                                const float cv = (kv * hl) * irr;
+                                fx += dx * cp + (vj.x - v.x) * cv;
+                                fy += dy * cp + (vj.y - v.y) * cv;
+                                fz += dz * cp + (vj.z - v.z) * cv;
+                            }
+                        }
+                    }
+            F = make_float3(fx * mass + S->gravity[0], fy * mass + S->gravity[1], fz * mass + S->gravity[2]);
+            if (R.use_sta) {
+                float3 c = fg_fluid_rigid_contact(S, it.scene, p, v, R.sta, false);
+                F.x += c.x; F.y += c.y; F.z += c.z;
+            }
+            if (R.use_dyn && (S->flags & FG_SCENE_HAS_RB)) {
+                float3 c = fg_fluid_rigid_contact(S, it.scene, p, v, R.dyn, true);
+                F.x += c.x; F.y += c.y; F.z += c.z;
+            }
+            const float3 wl = fg_walls(*S, make_float3(p.x, p.y, p.z), make_float3(v.x, v.y, v.z));
+            F.x += wl.x; F.y += wl.y; F.z += wl.z;
+            const float sp2 = F.x * F.x + F.y * F.y + F.z * F.z;
+            const float speed = sqrtf(sp2);
+            if (speed > S->vlimit) {
+                const float t = S->vlimit / speed;
+                F.x *= t; F.y *= t; F.z *= t;
+            }
+        }
+        const float dt = S->dt;
+        float4 nv;
+        nv.x = v.x + F.x * dt;
+        nv.y = v.y + F.y * dt;
+        nv.z = v.z + F.z * dt;
+        nv.w = v.w + 0.0f;
+        const uint32_t oi = __ldg(ids + i);
+        vel_out[oi] = nv;
+        if (pos_out && p.w > 0.0f) {
+            /* SPHIntegrateK fused: pos += vel * (dt / scale), unfused rounding */
+            const float c = S->dt_over_scale;
+            float4 np;
+            np.x = __fadd_rn(p.x, __fmul_rn(nv.x, c));
+            np.y = __fadd_rn(p.y, __fmul_rn(nv.y, c));
+            np.z = __fadd_rn(p.z, __fmul_rn(nv.z, c));
+            np.w = __fadd_rn(p.w, __fmul_rn(nv.w, c));
+            pos_out[oi] = np;
+        }
+    }
+}
+
+void launch_forces(const Launch &L, const float4 *spos, const float4 *svel, const float2 *dp, const uint32_t *start,
+                   const uint32_t *end, const uint32_t *ids, ForceOut out, const RigidGrid *rigid,
+                   const RigidGrid *statics, float mass_o, float visc_o, int use_o)
+{
+    if (!L.nwork) return;
+    RigidArgs R;
+    memset(&R, 0, sizeof(R));
+    if (rigid) { R.dyn = *rigid; R.use_dyn = 1; }
+    if (statics) { R.sta = *statics; R.use_sta = 1; }
+    k_forces<<<grid_for(L.nwork, 16), FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel,
+                                                               dp, start, end, ids, out.vel, out.pos, R, mass_o,
+                                                               visc_o, use_o);
+}
+
+/* SPHIntegrateK (K_FluidSim.cu:418-438): pos += vel*(dt/scale) for active
+ * particles, all four components, each operation rounded separately. */
+__global__ void __launch_bounds__(FG_CHUNK) k_integrate(const FgWork *__restrict__ work, uint32_t nwork,
+                                                       uint32_t n_single, const FgScene *__restrict__ table,
+                                                       const __grid_constant__ FgScene single,
+                                                       float4 *__restrict__ pos, const float4 *__restrict__ vel)
+{
+    for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+        FgWork it = fg_work(work, w, n_single);
+        if (threadIdx.x >= it.count) continue;
+        const FgScene *S = fg_scene(table, &single, it.scene);
+        const uint32_t i = it.first + threadIdx.x;
+        float4 p = pos[i];
+        if (p.w > 0.0f) {
+            const float4 v = __ldg(vel + i);
+            const float c = S->dt_over_scale;
+            p.x = __fadd_rn(p.x, __fmul_rn(v.x, c));
+            p.y = __fadd_rn(p.y, __fmul_rn(v.y, c));
+            p.z = __fadd_rn(p.z, __fmul_rn(v.z, c));
+            p.w = __fadd_rn(p.w, __fmul_rn(v.w, c));
+            pos[i] = p;
+        }
+    }
+}
+
+void launch_integrate(const Launch &L, float4 *pos, const float4 *vel)
+{
+    if (!L.nwork) return;
+    k_integrate<<<grid_for(L.nwork, 16), FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, pos,
+                                                                  vel);
+}
+
+} // namespace fg

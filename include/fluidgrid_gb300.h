@@ -1,0 +1,191 @@
+/* fluidgrid_gb300 -- C ABI of the GB300 SPH step engine.
+ *
+ * A world is a packed set of independent scenes that advance together, one
+ * step = the reference's HeterogeneousSimulator::doTimeStep for every scene
+ * (HeterogeneousSimulator.cpp:54-127) with the two-way rigid-body coupling of
+ * its commented block (:57-126, RigidBodySimulator.cpp:334-611):
+ *   hash -> stable key/index radix sort -> cell start/end + sorted gather ->
+ *   density -> [rigid spheres: transform+hash -> sort -> ranges -> contact
+ *   from fluid] -> pressure+viscosity+walls+contact forces with fused
+ *   integration -> FP64 per-body reduction + body integration.
+ * A world of one scene is the plain drop-in step; many scenes give the
+ * batched form (one launch per stage for all scenes).
+ *
+ * Every call returns an fg_status.  Plain pointers and sizes only; device
+ * buffers belong to the world, host buffers to the caller.  Calls on one
+ * world are not thread-safe; different worlds are independent.
+ */
+#ifndef FLUIDGRID_GB300_H
+#define FLUIDGRID_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *fg_stream_t; /* a cudaStream_t; NULL = the world creates its own */
+
+typedef enum fg_status {
+    FG_OK = 0,
+    FG_E_INVALID = 1,    /* bad argument */
+    FG_E_CUDA = 2,       /* CUDA runtime error (see fg_last_error) */
+    FG_E_OOM = 3,        /* device allocation failed */
+    FG_E_BUDGET = 4,     /* request exceeds the HBM budget */
+    FG_E_NONFINITE = 5,  /* a kernel produced NaN/Inf state */
+    FG_E_TIMEOUT = 6,    /* a bounded device wait gave up */
+    FG_E_STATE = 7,      /* call not valid in the current state */
+    FG_E_UNSUPPORTED = 8,
+    FG_E_NOLIB = 9       /* CUDA driver/device unavailable */
+} fg_status;
+
+/* One rigid body: surface spheres in body coordinates and its state.
+ * RigidBody (Simulators/RigidBody.cpp:55-126) + RigidBodySimulator::addElement
+ * (RigidBodySimulator.cpp:76-132). */
+typedef struct fg_body_desc {
+    uint32_t n_spheres;
+    const float *local_spheres; /* host float4[n_spheres]: x,y,z (w ignored) */
+    float mass;
+    float position[3];     /* centre of mass */
+    float orientation[4];  /* quaternion x,y,z,w */
+    float inv_inertia[9];  /* row-major body-frame inverse inertia */
+} fg_body_desc;
+
+/* One scene.  Fields mirror CommonFluidParams / FluidParams /
+ * CommonRigidBodyParams (ApplicationData.cuh:32-102) plus the constants the
+ * reference writes as literals in its kernels (defaults from
+ * fg_scene_desc_defaults equal those literals). */
+typedef struct fg_scene_desc {
+    uint32_t n_particles;
+    const float *positions;  /* host float4[n]: x,y,z,w (w > 0 = active) */
+    const float *velocities; /* host float4[n], or NULL for zero */
+    float cell_size[3];
+    int32_t bucket_size[3];  /* numBuckets = product */
+    float kernel_radius;
+    float velocity_limit;
+    float volume_min[3], volume_max[3];
+    float gravity[3];
+    float simulation_scale;
+    float dt;
+    float mass, rest_density, gas_constant, viscosity;
+    /* K_FluidSim.cu:289-293 literals */
+    float wall_distance, wall_stiffness, wall_damping;
+    float noslip_min[3], noslip_max[3];
+    float friction_kinetic, friction_static;
+    /* rigid bodies */
+    uint32_t n_bodies;
+    const fg_body_desc *bodies;
+    float fluid_radius;           /* fluid particle contact radius */
+    float rb_radius;              /* surface sphere radius (rigid grid cell) */
+    int32_t rb_bucket_size[3];
+    int32_t fluid_to_rb_relation[3];
+    int32_t rb_to_fluid_relation[3];
+    float contact_kspring, contact_kdamping;
+    float fluid_contact_eps;      /* 0.003 (K_FluidSim.cu:386) */
+    float rb_contact_eps;         /* 0.0001 (K_RigidBodySim.cu:87) */
+    int32_t rb_rb_contact;        /* sphere/sphere contact between bodies */
+    float rbrb_kspring, rbrb_kdamping, rbrb_eps; /* eps 0.001 (K_RigidBodySim.cu:42) */
+    float rb_gravity[4];
+    float rb_velocity_limit;
+    float rb_dt;
+    float rb_volume_min[3], rb_volume_max[3];
+} fg_scene_desc;
+
+void fg_scene_desc_defaults(fg_scene_desc *d);
+
+typedef struct fg_world fg_world;
+
+int fg_world_create(const fg_scene_desc *scenes, uint32_t nscenes, fg_stream_t stream, fg_world **out);
+int fg_world_destroy(fg_world *w);
+
+/* Enqueue nsteps steps on the world's stream (CUDA-graph replay after the
+ * first call).  Returns without waiting. */
+int fg_world_step(fg_world *w, uint32_t nsteps);
+/* Wait for the world's stream; returns FG_E_NONFINITE if the last
+ * fg_world_check found NaN/Inf, FG_E_CUDA on a CUDA error. */
+int fg_world_sync(fg_world *w);
+/* Scan every scene's state for NaN/Inf (enqueued; result seen at sync). */
+int fg_world_check(fg_world *w);
+
+/* Whole-world state in packed scene-major order (host float4 arrays of
+ * fg_world_particles() entries).  Copies are enqueued on the world's stream;
+ * pinned host memory makes them asynchronous. */
+int fg_world_upload(fg_world *w, const float *pos4, const float *vel4);
+int fg_world_download(fg_world *w, float *pos4, float *vel4);
+/* One scene's state (scene-local arrays of n_particles entries). */
+int fg_world_scene_upload(fg_world *w, uint32_t scene, const float *pos4, const float *vel4);
+int fg_world_scene_download(fg_world *w, uint32_t scene, float *pos4, float *vel4);
+
+uint32_t fg_world_particles(const fg_world *w);
+uint32_t fg_world_scenes(const fg_world *w);
+uint32_t fg_world_spheres(const fg_world *w);
+uint32_t fg_world_bodies(const fg_world *w);
+/* scene layout: first particle, particle count, first global bucket,
+ * buckets, first sphere, spheres, first body, bodies */
+int fg_world_scene_layout(const fg_world *w, uint32_t scene, uint32_t out[8]);
+
+/* Device buffers of a world (for drop-in callers and parity checks). */
+typedef enum fg_buffer_id {
+    FG_BUF_POS = 0, FG_BUF_VEL, FG_BUF_KEYS_UNSORTED, FG_BUF_KEYS, FG_BUF_IDS, FG_BUF_START, FG_BUF_END,
+    FG_BUF_SPOS, FG_BUF_SVEL, FG_BUF_DP,
+    FG_BUF_RB_LOCAL, FG_BUF_RB_WORLD, FG_BUF_RB_KEYS_UNSORTED, FG_BUF_RB_KEYS, FG_BUF_RB_IDS, FG_BUF_RB_START,
+    FG_BUF_RB_END, FG_BUF_RB_SPOS, FG_BUF_RB_FORCE, FG_BUF_RB_TORQUE,
+    FG_BUF_BODY_X, FG_BUF_BODY_V, FG_BUF_BODY_Q, FG_BUF_BODY_L, FG_BUF_BODY_FSUM, FG_BUF_BODY_TSUM,
+    FG_BUF_BODY_XF, FG_BUF_BODY_VF, FG_BUF_BODY_QF, FG_BUF_BODY_MASS, FG_BUF_BODY_INV_INERTIA,
+    FG_BUF_COUNT
+} fg_buffer_id;
+int fg_world_buffer(fg_world *w, int id, void **dev_ptr, size_t *bytes);
+
+/* Stage control for parity checks: run only the stages whose bit is set in
+ * `mask` for the next fg_world_step calls (default: all).  Bits follow the
+ * step order below. */
+enum {
+    FG_STAGE_HASH = 1, FG_STAGE_SORT = 2, FG_STAGE_RANGES = 4, FG_STAGE_DENSITY = 8,
+    FG_STAGE_RB_GRID = 16, FG_STAGE_RB_CONTACT = 32, FG_STAGE_FORCES = 64, FG_STAGE_BODIES = 128,
+    FG_STAGE_ALL = 255
+};
+int fg_world_set_stages(fg_world *w, uint32_t mask);
+/* 0 = fused forces+integration (default), 1 = separate SPHIntegrateK pass */
+int fg_world_set_fused_integrate(fg_world *w, int fused);
+/* radix digit width 1..8 (autotuned default) */
+int fg_world_set_sort_digit_bits(fg_world *w, uint32_t bits);
+/* 1 = capture steps in a CUDA graph (default), 0 = direct launches */
+int fg_world_set_graphs(fg_world *w, int on);
+/* number of kernel launches one step enqueues */
+uint32_t fg_world_launches_per_step(const fg_world *w);
+
+/* ---- measurement (CUDA events on the world's stream) ----
+ * One step in direct-launch mode with an event pair around each stage,
+ * after rewriting a flush_bytes buffer (0 = no flush); stage_ms[k] receives
+ * the time of stage bit k (0 if not run). */
+int fg_world_stage_profile(fg_world *w, size_t flush_bytes, float stage_ms[8]);
+/* nsteps steps (graph replay), each bracketed by events; before each step a
+ * flush_bytes buffer is rewritten so no step starts with a warm L2.
+ * ms[k] = duration of step k. */
+int fg_world_timed_steps(fg_world *w, uint32_t nsteps, size_t flush_bytes, float *ms);
+/* End to end through host memory: per step, copy positions and velocities
+ * from host_pos4/host_vel4 to the device, step, copy them back to
+ * out_pos4/out_vel4; ms[k] = device time of step k including both copies.
+ * Pinned host buffers (fg_host_alloc) keep the copies asynchronous. */
+int fg_world_e2e_steps(fg_world *w, uint32_t nsteps, const float *host_pos4, const float *host_vel4,
+                       float *out_pos4, float *out_vel4, float *ms);
+void *fg_host_alloc(size_t bytes); /* pinned host memory, NULL on failure */
+int fg_host_free(void *p);
+int fg_set_device(int device);
+/* FP32 FMA throughput of the current device (register-resident loop), in
+ * TFLOP/s; used as the FP32 roofline denominator. */
+int fg_probe_fp32_peak(float *tflops);
+
+/* Small helpers so callers without a CUDA runtime binding can move data. */
+int fg_memcpy_d2h(void *dst, const void *src, size_t bytes);
+int fg_memcpy_h2d(void *dst, const void *src, size_t bytes);
+int fg_device_synchronize(void);
+const char *fg_last_error(void);
+const char *fg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
