@@ -186,6 +186,7 @@ static void build_work(std::vector<FgWork> &wt, uint32_t scene, uint32_t first, 
 int World::create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st)
 {
     nscenes = ns;
+    (void)sm_count(); /* cache the device query outside any graph capture */
     if (st) {
         stream = st;
         own_stream = false;
