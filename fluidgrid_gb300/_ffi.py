@@ -86,6 +86,7 @@ C_ABI_SYMBOLS = [
     "fg_world_buffer", "fg_world_set_stages", "fg_world_set_fused_integrate", "fg_world_set_sort_digit_bits",
     "fg_world_set_graphs", "fg_world_launches_per_step", "fg_world_stage_profile", "fg_world_timed_steps",
     "fg_world_e2e_steps", "fg_host_alloc", "fg_host_free", "fg_set_device", "fg_probe_fp32_peak",
+    "fg_sort_pairs_noalloc",
     "fg_memcpy_d2h", "fg_memcpy_h2d",
     "fg_device_synchronize", "fg_last_error", "fg_version"]
 REFERENCE_SYMBOLS = [
@@ -144,6 +145,7 @@ def load():
     L.fg_host_free.argtypes = [VP]
     L.fg_set_device.argtypes = [ctypes.c_int]
     L.fg_probe_fp32_peak.argtypes = [P(c_f)]
+    L.fg_sort_pairs_noalloc.argtypes = [VP, VP, c_u32, c_u32, VP]
     L.fg_memcpy_d2h.argtypes = [VP, VP, ctypes.c_size_t]
     L.fg_memcpy_h2d.argtypes = [VP, VP, ctypes.c_size_t]
     L.fg_last_error.restype = ctypes.c_char_p

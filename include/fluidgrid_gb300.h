@@ -177,6 +177,19 @@ int fg_set_device(int device);
  * TFLOP/s; used as the FP32 roofline denominator. */
 int fg_probe_fp32_peak(float *tflops);
 
+/* Stable in-place sort of n (key, value) pairs by the low keyBits bits of the
+ * key -- the same result as fgc_sort_pairs -- without allocating: its scratch
+ * is a fixed ~8.65 MB array inside the library (held on every GPU that loads
+ * it), for callers that cannot call cudaMalloc/cudaFree while they sort (a
+ * host that gives all device memory to its own pool, a step loop that must
+ * not wait for the allocator).  No counterpart in the reference.
+ * n <= 1,048,576 (larger n -> FG_E_INVALID).  All calls share the scratch:
+ * calls that overlap on the GPU race, so serialise them.  The first call on a
+ * device looks up the scratch address; make it before any stream capture.
+ * Work is enqueued on `stream` (NULL = legacy default stream). */
+int fg_sort_pairs_noalloc(unsigned int *keys, unsigned int *values, unsigned int keyBits, unsigned int n,
+                          fg_stream_t stream);
+
 /* Small helpers so callers without a CUDA runtime binding can move data. */
 int fg_memcpy_d2h(void *dst, const void *src, size_t bytes);
 int fg_memcpy_h2d(void *dst, const void *src, size_t bytes);
