@@ -262,6 +262,10 @@ int World::create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st)
     if ((r = A((void **)&rs.keys_alt, 4 * M))) return r;
     if ((r = A((void **)&rs.vals_alt, 4 * M))) return r;
     if ((r = A((void **)&rs.hist, 4 * radix_hist_words((uint32_t)M)))) return r;
+    if ((r = A((void **)&nbr.idx, 4 * (size_t)FG_NBR_MAX * N))) return r;
+    if ((r = A((void **)&nbr.cnt, 4 * N))) return r;
+    if ((r = A((void **)&nbr.rec, 32 * N))) return r;
+    nbr.stride = (uint32_t)N;
     if ((r = A((void **)&status_d, 64))) return r;
     CK(cudaMemsetAsync(status_d, 0, 64, stream));
     CK(cudaMemsetAsync(dp, 0, 8 * N, stream));
@@ -416,7 +420,7 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
     }
     if (stages & FG_STAGE_DENSITY) {
         mark(3, 0);
-        launch_density(L, spos, start, end, dp, 0.f, 0.f, 0.f, 0);
+        launch_density(L, spos, start, end, dp, 0.f, 0.f, 0.f, 0, svel, &nbr);
         mark(3, 1);
         launches++;
     }
@@ -456,7 +460,7 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         ForceOut o;
         o.vel = vel;
         o.pos = fused_integrate ? pos : nullptr;
-        launch_forces(L, spos, svel, dp, start, end, ids, o, rb ? &G : nullptr, nullptr, 0.f, 0.f, 0);
+        launch_forces(L, spos, svel, dp, start, end, ids, o, rb ? &G : nullptr, nullptr, 0.f, 0.f, 0, &nbr);
         launches++;
         if (!fused_integrate) {
             launch_integrate(L, pos, vel);

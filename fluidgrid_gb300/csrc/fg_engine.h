@@ -32,6 +32,7 @@ struct World {
     float2 *dp = nullptr;
     uint32_t *keys_u = nullptr, *keys = nullptr, *ids = nullptr, *start = nullptr, *end = nullptr;
     RadixScratch rs{nullptr, nullptr, nullptr};
+    NbrList nbr{nullptr, nullptr, nullptr, 0}; /* density -> forces neighbour lists */
     /* rigid */
     float4 *rb_local = nullptr, *rb_world = nullptr, *rb_spos = nullptr, *rb_force = nullptr, *rb_torque = nullptr;
     uint32_t *rb_keys_u = nullptr, *rb_keys = nullptr, *rb_ids = nullptr, *rb_start = nullptr, *rb_end = nullptr;

@@ -46,8 +46,24 @@ void launch_cell_ranges(const uint32_t *keys, const uint32_t *ids, const float4 
                         uint32_t *start, uint32_t *end, float4 *spos, float4 *svel, uint32_t n, cudaStream_t st);
 
 /* ---- SPH (fg_sph.cu) ---- */
+
+/* In-range neighbour lists recorded by the density pass and consumed by the
+ * force pass.  Slot k of sorted particle i is idx[k * stride + i] (SoA, so a
+ * warp's stores and loads of one slot coalesce); cnt[i] is the number of
+ * in-range bucket visits (may exceed FG_NBR_MAX, then forces re-walk the
+ * buckets).  rec[2i] = (x, y, z, rho_i), rec[2i+1] = (vx, vy, vz, P_i): one
+ * 32-byte sector per neighbour gather. */
+#define FG_NBR_MAX 64u
+struct NbrList {
+    uint32_t *idx;
+    uint32_t *cnt;
+    float4 *rec;
+    uint32_t stride;
+};
+
 void launch_density(const Launch &L, const float4 *spos, const uint32_t *start, const uint32_t *end, float2 *dp,
-                    float gas_override, float rest_override, float mass_override, int use_override);
+                    float gas_override, float rest_override, float mass_override, int use_override,
+                    const float4 *svel = nullptr, const NbrList *list = nullptr);
 
 struct RigidGrid {
     const float4 *spos;     /* sorted sphere positions, w = body index */
@@ -66,7 +82,8 @@ struct ForceOut {
 
 void launch_forces(const Launch &L, const float4 *spos, const float4 *svel, const float2 *dp, const uint32_t *start,
                    const uint32_t *end, const uint32_t *ids, ForceOut out, const RigidGrid *rigid,
-                   const RigidGrid *statics, float mass_override, float visc_override, int use_override);
+                   const RigidGrid *statics, float mass_override, float visc_override, int use_override,
+                   const NbrList *list = nullptr);
 
 void launch_integrate(const Launch &L, float4 *pos, const float4 *vel);
 

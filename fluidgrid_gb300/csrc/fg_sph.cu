@@ -16,9 +16,17 @@
  * the tolerances the parity tests state.
  *
  * One thread per particle in sorted order: neighbouring lanes share cells,
- * so neighbour loads broadcast from L1 and sorted float4 loads coalesce. */
+ * so neighbour loads broadcast from L1 and sorted float4 loads coalesce.
+ * In the world pipeline the density pass is the only one that walks the
+ * ~216 candidates of the 27 buckets: it stages each particle's in-range
+ * neighbours (in visit order, duplicates included) in shared memory and
+ * writes them out coalesced, together with a packed 32-byte record per
+ * particle.  The force pass then loops over ~30 listed neighbours per
+ * particle with all lanes busy, instead of re-walking 216 candidates where
+ * almost every warp iteration would run the pair math for a few lanes. */
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 #include "fg_device.cuh"
 #include "fg_kernels.h"
 
@@ -36,61 +44,111 @@ struct Kahan {
     }
 };
 
+/* Visit the particles of the 27 neighbour buckets in the reference's order
+ * (z outer, x inner, each from -1 to 1; ascending sorted index inside a
+ * bucket).  Fully unrolled so the per-axis hashes live in registers. */
+template <typename Fn>
+__device__ __forceinline__ void fg_walk27(float px, float py, float pz, const FgScene *S,
+                                          const uint32_t *__restrict__ start, const uint32_t *__restrict__ end,
+                                          Fn &&fn)
+{
+    uint32_t hx[3], hy[3], hz[3];
+    fg_neighbour_hashes(px, py, pz, S->cell, hx, hy, hz);
+    const uint32_t nb = S->nb, mask = S->nb_mask, bb = S->bucket_base;
+#pragma unroll
+    for (int z = 0; z < 3; z++)
+#pragma unroll
+        for (int y = 0; y < 3; y++)
+#pragma unroll
+            for (int x = 0; x < 3; x++) {
+                const uint32_t b = bb + fg_bucket(hx[x], hy[y], hz[z], nb, mask);
+                const uint32_t st = __ldg(start + b);
+                if (st == FG_EMPTY) continue;
+                const uint32_t en = __ldg(end + b);
+                for (uint32_t j = st; j < en; j++) fn(j);
+            }
+}
+
+template <bool LIST>
 __global__ void __launch_bounds__(FG_CHUNK) k_density(const FgWork *__restrict__ work, uint32_t nwork,
                                                      uint32_t n_single, const FgScene *__restrict__ table,
                                                      const __grid_constant__ FgScene single,
                                                      const float4 *__restrict__ spos,
+                                                     const float4 *__restrict__ svel,
                                                      const uint32_t *__restrict__ start,
                                                      const uint32_t *__restrict__ end, float2 *__restrict__ dp,
-                                                     float gas_o, float rest_o, float mass_o, int use_o)
+                                                     float gas_o, float rest_o, float mass_o, int use_o,
+                                                     const __grid_constant__ NbrList list)
 {
+    __shared__ uint32_t s_nbr[LIST ? FG_NBR_MAX : 1][FG_CHUNK];
+    const uint32_t tid = threadIdx.x;
     for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
         FgWork it = fg_work(work, w, n_single);
-        if (threadIdx.x >= it.count) continue;
+        const bool valid = tid < it.count;
         const FgScene *S = fg_scene(table, &single, it.scene);
-        const uint32_t i = it.first + threadIdx.x;
-        const float4 p = spos[i];
-        if (!(p.w > 0.0f)) continue; /* inactive: density not written */
-        const float scale = S->scale, h2 = S->h2;
-        const uint32_t nb = S->nb, mask = S->nb_mask, bb = S->bucket_base;
-        uint32_t hx[3], hy[3], hz[3];
-        fg_neighbour_hashes(p.x, p.y, p.z, S->cell, hx, hy, hz);
-        const float px = p.x * scale, py = p.y * scale, pz = p.z * scale;
-        Kahan acc = {0.f, 0.f};
-#pragma unroll 1
-        for (int z = 0; z < 3; z++)
-#pragma unroll 1
-            for (int y = 0; y < 3; y++)
-#pragma unroll 1
-                for (int x = 0; x < 3; x++) {
-                    const uint32_t b = bb + fg_bucket(hx[x], hy[y], hz[z], nb, mask);
-                    const uint32_t st = __ldg(start + b);
-                    if (st == FG_EMPTY) continue;
-                    const uint32_t en = __ldg(end + b);
-                    for (uint32_t j = st; j < en; j++) {
-                        const float4 q = __ldg(spos + j);
-                        const float dx = px - q.x * scale, dy = py - q.y * scale, dz = pz - q.z * scale;
-                        const float r2 = dx * dx + dy * dy + dz * dz;
-                        if (r2 < h2) {
-                            const float t = h2 - r2;
-                            acc.add(t * t * t);
-                        }
+        const uint32_t i = it.first + tid;
+        const float4 p = valid ? spos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool active = valid && p.w > 0.0f; /* inactive: density not written */
+        uint32_t cnt = 0;
+        if (active) {
+            const float scale = S->scale, h2 = S->h2;
+            const float px = p.x * scale, py = p.y * scale, pz = p.z * scale;
+            Kahan acc = {0.f, 0.f};
+            fg_walk27(p.x, p.y, p.z, S, start, end, [&](uint32_t j) {
+                const float4 q = __ldg(spos + j);
+                const float dx = fmaf(-q.x, scale, px), dy = fmaf(-q.y, scale, py), dz = fmaf(-q.z, scale, pz);
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                if (r2 < h2) {
+                    const float t = h2 - r2;
+                    acc.add(t * t * t);
+                    if (LIST) {
+                        if (cnt < FG_NBR_MAX) s_nbr[cnt][tid] = j;
+                        cnt++;
                     }
                 }
-        const float mass = use_o ? mass_o : S->mass;
-        const float gas = use_o ? gas_o : S->gas;
-        const float rest = use_o ? rest_o : S->rest;
-        const float rho = (mass * S->kpoly6) * acc.s;
-        dp[i] = make_float2(fmaxf(1.0f, rho), gas * (rho - rest));
+            });
+            const float mass = use_o ? mass_o : S->mass;
+            const float gas = use_o ? gas_o : S->gas;
+            const float rest = use_o ? rest_o : S->rest;
+            const float rho = (mass * S->kpoly6) * acc.s;
+            const float2 d = make_float2(fmaxf(1.0f, rho), gas * (rho - rest));
+            dp[i] = d;
+            if (LIST) {
+                const float4 v = __ldg(svel + i);
+                list.rec[2 * i] = make_float4(p.x, p.y, p.z, d.x);
+                list.rec[2 * i + 1] = make_float4(v.x, v.y, v.z, d.y);
+            }
+        } else if (LIST && valid) {
+            /* inactive particles stay neighbours with their stale density */
+            const float2 d = dp[i];
+            const float4 v = __ldg(svel + i);
+            list.rec[2 * i] = make_float4(p.x, p.y, p.z, d.x);
+            list.rec[2 * i + 1] = make_float4(v.x, v.y, v.z, d.y);
+        }
+        if (LIST) {
+            if (valid) list.cnt[i] = cnt;
+            const uint32_t m = cnt < FG_NBR_MAX ? cnt : FG_NBR_MAX;
+            const uint32_t wm = __reduce_max_sync(0xffffffffu, m);
+            for (uint32_t k = 0; k < wm; k++)
+                if (k < m) list.idx[(size_t)k * list.stride + i] = s_nbr[k][tid];
+        }
     }
 }
 
 void launch_density(const Launch &L, const float4 *spos, const uint32_t *start, const uint32_t *end, float2 *dp,
-                    float gas_o, float rest_o, float mass_o, int use_o)
+                    float gas_o, float rest_o, float mass_o, int use_o, const float4 *svel, const NbrList *list)
 {
     if (!L.nwork) return;
-    k_density<<<grid_for(L.nwork, 16), FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos,
-                                                                start, end, dp, gas_o, rest_o, mass_o, use_o);
+    const uint32_t g = grid_for(L.nwork, 16);
+    if (list) {
+        k_density<true><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, start,
+                                                      end, dp, gas_o, rest_o, mass_o, use_o, *list);
+    } else {
+        NbrList none;
+        memset(&none, 0, sizeof(none));
+        k_density<false><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, start,
+                                                       end, dp, gas_o, rest_o, mass_o, use_o, none);
+    }
 }
 
 /* Rigid-sphere contact of one fluid particle against a rigid grid
@@ -141,6 +199,26 @@ struct RigidArgs {
     int use_dyn, use_sta;
 };
 
+/* Pressure + viscosity of neighbour j on i (SPHCalculatePressureForceD +
+ * SPHCalculateViscosityForceD): d = p_i - p_j (scaled), r2 = |d|^2 <= h^2. */
+__device__ __forceinline__ void fg_pair(float &fx, float &fy, float &fz, float dx, float dy, float dz, float r2,
+                                        float h, float kspiky, float kv, float rho_i, float P_i, float4 vi,
+                                        float rho_j, float P_j, float4 vj)
+{
+    const float il = rsqrtf(r2);
+    const float l = r2 * il;
+    const float hl = h - l;
+    const float irr = __frcp_rn(rho_i * rho_j);
+    /* pressure: -(d/l) kSpiky (h-l)^2 (Pi+Pj)/(rho_i rho_j) */
+    const float cp = -(kspiky * hl * hl) * ((P_i + P_j) * irr) * il;
+    /* viscosity: (vj-vi)/(rho_i rho_j) kVisc (h-l) mu */
+    const float cv = (kv * hl) * irr;
+    fx += dx * cp + (vj.x - vi.x) * cv;
+    fy += dy * cp + (vj.y - vi.y) * cv;
+    fz += dz * cp + (vj.z - vi.z) * cv;
+}
+
+template <bool LIST>
 __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ work, uint32_t nwork,
                                                     uint32_t n_single, const FgScene *__restrict__ table,
                                                     const __grid_constant__ FgScene single,
@@ -151,7 +229,7 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                                                     const uint32_t *__restrict__ ids, float4 *__restrict__ vel_out,
                                                     float4 *__restrict__ pos_out,
                                                     const __grid_constant__ RigidArgs R, float mass_o, float visc_o,
-                                                    int use_o)
+                                                    int use_o, const __grid_constant__ NbrList list)
 {
     for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
         FgWork it = fg_work(work, w, n_single);
@@ -163,47 +241,54 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
         float3 F = make_float3(0.f, 0.f, 0.f);
         if (p.w > 0.0f) {
             const float scale = S->scale, h = S->h, h2 = S->h2;
-            const uint32_t nb = S->nb, mask = S->nb_mask, bb = S->bucket_base;
             const float mass = use_o ? mass_o : S->mass;
             const float visc = use_o ? visc_o : S->visc;
-            const float2 di = dp[i];
             const float kspiky = S->kspiky, kv = S->kvisc * visc;
-            uint32_t hx[3], hy[3], hz[3];
-            fg_neighbour_hashes(p.x, p.y, p.z, S->cell, hx, hy, hz);
             const float px = p.x * scale, py = p.y * scale, pz = p.z * scale;
             float fx = 0.f, fy = 0.f, fz = 0.f;
-#pragma unroll 1
-            for (int z = 0; z < 3; z++)
-#pragma unroll 1
-                for (int y = 0; y < 3; y++)
-#pragma unroll 1
-                    for (int x = 0; x < 3; x++) {
-                        const uint32_t b = bb + fg_bucket(hx[x], hy[y], hz[z], nb, mask);
-                        const uint32_t st = __ldg(start + b);
-                        if (st == FG_EMPTY) continue;
-                        const uint32_t en = __ldg(end + b);
-                        for (uint32_t j = st; j < en; j++) {
-                            if (j == i) continue;
-                            const float4 q = __ldg(spos + j);
-                            const float dx = px - q.x * scale, dy = py - q.y * scale, dz = pz - q.z * scale;
-                            const float r2 = dx * dx + dy * dy + dz * dz;
-                            if (r2 <= h2) {
-                                const float4 vj = __ldg(svel + j);
-                                const float2 dj = __ldg(dp + j);
-                                const float il = rsqrtf(r2);
-                                const float l = r2 * il;
-                                const float hl = h - l;
-                                const float irr = __frcp_rn(di.x * dj.x);
-                                /* pressure: -(d/l) kSpiky (h-l)^2 (Pi+Pj)/(rho_i rho_j) */
-                                const float cp = -(kspiky * hl * hl) * ((di.y + dj.y) * irr) * il;
-                                /* viscosity: (vj-vi)/(rho_i rho_j) kVisc (h-l) mu */
-                                const float cv = (kv * hl) * irr;
-                                fx += dx * cp + (vj.x - v.x) * cv;
-                                fy += dy * cp + (vj.y - v.y) * cv;
-                                fz += dz * cp + (vj.z - v.z) * cv;
-                            }
-                        }
+            if (LIST) {
+                const float4 r0 = list.rec[2 * i], r1 = list.rec[2 * i + 1];
+                const float rho_i = r0.w, P_i = r1.w;
+                const uint32_t c = list.cnt[i];
+                if (c <= FG_NBR_MAX) {
+                    const uint32_t *nl = list.idx + i;
+                    for (uint32_t k = 0; k < c; k++) {
+                        const uint32_t j = __ldg(nl + (size_t)k * list.stride);
+                        if (j == i) continue;
+                        const float4 q0 = __ldg(list.rec + 2 * j), q1 = __ldg(list.rec + 2 * j + 1);
+                        const float dx = fmaf(-q0.x, scale, px), dy = fmaf(-q0.y, scale, py),
+                                    dz = fmaf(-q0.z, scale, pz);
+                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        fg_pair(fx, fy, fz, dx, dy, dz, r2, h, kspiky, kv, rho_i, P_i, v, q0.w, q1.w, q1);
                     }
+                } else {
+                    /* more in-range visits than list slots: walk the buckets */
+                    fg_walk27(p.x, p.y, p.z, S, start, end, [&](uint32_t j) {
+                        if (j == i) return;
+                        const float4 q0 = __ldg(list.rec + 2 * j);
+                        const float dx = fmaf(-q0.x, scale, px), dy = fmaf(-q0.y, scale, py),
+                                    dz = fmaf(-q0.z, scale, pz);
+                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        if (r2 <= h2) {
+                            const float4 q1 = __ldg(list.rec + 2 * j + 1);
+                            fg_pair(fx, fy, fz, dx, dy, dz, r2, h, kspiky, kv, rho_i, P_i, v, q0.w, q1.w, q1);
+                        }
+                    });
+                }
+            } else {
+                const float2 di = dp[i];
+                fg_walk27(p.x, p.y, p.z, S, start, end, [&](uint32_t j) {
+                    if (j == i) return;
+                    const float4 q = __ldg(spos + j);
+                    const float dx = fmaf(-q.x, scale, px), dy = fmaf(-q.y, scale, py), dz = fmaf(-q.z, scale, pz);
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    if (r2 <= h2) {
+                        const float4 vj = __ldg(svel + j);
+                        const float2 dj = __ldg(dp + j);
+                        fg_pair(fx, fy, fz, dx, dy, dz, r2, h, kspiky, kv, di.x, di.y, v, dj.x, dj.y, vj);
+                    }
+                });
+            }
             F = make_float3(fx * mass + S->gravity[0], fy * mass + S->gravity[1], fz * mass + S->gravity[2]);
             if (R.use_sta) {
                 float3 c = fg_fluid_rigid_contact(S, it.scene, p, v, R.sta, false);
@@ -245,16 +330,24 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
 
 void launch_forces(const Launch &L, const float4 *spos, const float4 *svel, const float2 *dp, const uint32_t *start,
                    const uint32_t *end, const uint32_t *ids, ForceOut out, const RigidGrid *rigid,
-                   const RigidGrid *statics, float mass_o, float visc_o, int use_o)
+                   const RigidGrid *statics, float mass_o, float visc_o, int use_o, const NbrList *list)
 {
     if (!L.nwork) return;
     RigidArgs R;
     memset(&R, 0, sizeof(R));
     if (rigid) { R.dyn = *rigid; R.use_dyn = 1; }
     if (statics) { R.sta = *statics; R.use_sta = 1; }
-    k_forces<<<grid_for(L.nwork, 16), FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel,
-                                                               dp, start, end, ids, out.vel, out.pos, R, mass_o,
-                                                               visc_o, use_o);
+    const uint32_t g = grid_for(L.nwork, 16);
+    if (list) {
+        k_forces<true><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, dp, start,
+                                                     end, ids, out.vel, out.pos, R, mass_o, visc_o, use_o, *list);
+    } else {
+        NbrList none;
+        memset(&none, 0, sizeof(none));
+        k_forces<false><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, dp,
+                                                      start, end, ids, out.vel, out.pos, R, mass_o, visc_o, use_o,
+                                                      none);
+    }
 }
 
 /* SPHIntegrateK (K_FluidSim.cu:418-438): pos += vel*(dt/scale) for active
