@@ -66,6 +66,12 @@ __device__ __forceinline__ uint32_t fg_axis_hash_rel(float p, float cell, int o,
     return (uint32_t)fg_axis_index(__fadd_rn(p, off), cell) * prime;
 }
 
+/* select one of three register values without local-memory indexing */
+__device__ __forceinline__ uint32_t fg_sel3(uint32_t a0, uint32_t a1, uint32_t a2, int k)
+{
+    return k == 0 ? a0 : (k == 1 ? a1 : a2);
+}
+
 /* ------------------------------------------------------- work items */
 
 /* Resolve work item w to (scene, first, count).  With no table, the single

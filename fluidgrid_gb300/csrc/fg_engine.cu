@@ -76,8 +76,10 @@ int World::alloc(void **p, size_t bytes)
 World::~World()
 {
     if (flush_buf) cudaFree(flush_buf);
-    if (graph_exec) cudaGraphExecDestroy(graph_exec);
-    if (graph) cudaGraphDestroy(graph);
+    for (auto &g : graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        if (g.graph) cudaGraphDestroy(g.graph);
+    }
     for (void *p : allocs) cudaFree(p);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
@@ -266,8 +268,19 @@ int World::create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st)
     if ((r = A((void **)&nbr.cnt, 4 * N))) return r;
     if ((r = A((void **)&nbr.rec, 32 * N))) return r;
     nbr.stride = (uint32_t)N;
+    if ((r = A((void **)&runs, 4 * N))) return r;
+    if ((r = A((void **)&nruns, 16))) return r;
+    if ((r = A((void **)&inv, 4 * N))) return r;
+    if ((r = A((void **)&tord, 4 * N))) return r;
+    {
+        const uint32_t sbits = ceil_log2(ns);
+        order_bits = std::min<uint32_t>(10u, (32u - sbits) / 3u);
+        order_scene_shift = 3u * order_bits;
+        order_key_bits = order_scene_shift + sbits;
+    }
     if ((r = A((void **)&status_d, 64))) return r;
     CK(cudaMemsetAsync(status_d, 0, 64, stream));
+    pair_counter = (unsigned long long *)(status_d + 8); /* 8-byte aligned slot of the status block */
     CK(cudaMemsetAsync(dp, 0, 8 * N, stream));
     CK(cudaMemsetAsync(vel, 0, 16 * N, stream));
     CK(cudaMemsetAsync(end, 0, 4 * (size_t)std::max<uint32_t>(total_buckets, 1), stream));
@@ -414,13 +427,23 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
     if (stages & FG_STAGE_RANGES) {
         mark(2, 0);
         cudaMemsetAsync(start, 0xff, 4 * (size_t)total_buckets, stream);
-        launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream);
+        if (use_cc) {
+            cudaMemsetAsync(nruns, 0, 4, stream);
+            launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv, runs, nruns);
+        } else {
+            launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv);
+        }
         mark(2, 1);
         launches += 1;
     }
     if (stages & FG_STAGE_DENSITY) {
         mark(3, 0);
-        launch_density(L, spos, start, end, dp, 0.f, 0.f, 0.f, 0, svel, &nbr);
+        if (use_cc)
+            launch_density_cc(single ? nullptr : scenes_d, &scenes_h[0], nscenes, runs, nruns, keys, spos, svel, start,
+                              end, dp, nbr.rec, n, stream);
+        else
+            launch_density(L, spos, start, end, dp, 0.f, 0.f, 0.f, 0, svel, use_list ? &nbr : nullptr,
+                           target_order(), pair_counter);
         mark(3, 1);
         launches++;
     }
@@ -460,7 +483,12 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         ForceOut o;
         o.vel = vel;
         o.pos = fused_integrate ? pos : nullptr;
-        launch_forces(L, spos, svel, dp, start, end, ids, o, rb ? &G : nullptr, nullptr, 0.f, 0.f, 0, &nbr);
+        if (use_cc)
+            launch_forces_cc(single ? nullptr : scenes_d, &scenes_h[0], nscenes, runs, nruns, keys, spos, svel,
+                             nbr.rec, start, end, ids, o, rb ? &G : nullptr, n, stream);
+        else
+            launch_forces(L, spos, svel, dp, start, end, ids, o, rb ? &G : nullptr, nullptr, 0.f, 0.f, 0,
+                          use_list ? &nbr : nullptr, target_order());
         launches++;
         if (!fused_integrate) {
             launch_integrate(L, pos, vel);
@@ -484,33 +512,129 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
     return launches;
 }
 
-int World::step(uint32_t nsteps)
+/* Spatial target order from the current particle positions: Morton keys of
+ * the unsorted particles, stable sort by key with particle ids as values.
+ * The sorted-key buffers of the step are free here (the step rewrites them
+ * before reading), so they serve as key scratch. */
+void World::enqueue_order_refresh()
 {
-    if (!use_graphs) {
-        for (uint32_t k = 0; k < nsteps; k++) enqueue_step();
-        cudaError_t e = cudaPeekAtLastError();
-        if (e != cudaSuccess) {
-            set_error("step", e);
-            return FG_E_CUDA;
+    if (!n) return;
+    launch_morton_keys(fluid_launch(), pos, keys, order_bits, order_scene_shift);
+    radix_sort(keys, nullptr, keys_u, tord, n, order_key_bits, digit_bits, rs, stream);
+    order_valid = true;
+}
+
+uint32_t World::graph_signature() const
+{
+    return (stages & 0xffu) | (fused_integrate ? 0x100u : 0u) | (digit_bits << 9) | (use_list ? 0x10000u : 0u) |
+           ((use_order && order_valid) ? 0x20000u : 0u) | (use_cc ? 0x40000u : 0u);
+}
+
+int World::graph_for_current(cudaGraphExec_t *out)
+{
+    const uint32_t sig = graph_signature();
+    for (auto &g : graphs)
+        if (g.sig == sig) {
+            *out = g.exec;
+            return FG_OK;
         }
+    CachedGraph g{sig, nullptr, nullptr};
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step();
+    cudaError_t e = cudaStreamEndCapture(stream, &g.graph);
+    if (e != cudaSuccess) {
+        set_error("cudaStreamEndCapture", e);
+        return FG_E_CUDA;
+    }
+    e = cudaGraphInstantiate(&g.exec, g.graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g.graph);
+        set_error("cudaGraphInstantiate", e);
+        return FG_E_CUDA;
+    }
+    graphs.push_back(g);
+    *out = g.exec;
+    return FG_OK;
+}
+
+/* One autotuning round: each candidate kernel runs one real step bracketed
+ * by events (the state advances as in any step); the fastest is kept. */
+int World::tune_steps(uint32_t *done)
+{
+    int cands[3], nc = 0;
+    for (int k = 0; k < 3; k++)
+        if (tune_kernels & (1u << k)) cands[nc++] = k;
+    if (nc < 2) {
+        *done = 0;
         return FG_OK;
     }
-    if (!graph_exec || graph_stages != stages || graph_fused != fused_integrate || graph_digits != digit_bits) {
-        if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
-        if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
-        CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        enqueue_step();
-        cudaError_t e = cudaStreamEndCapture(stream, &graph);
-        if (e != cudaSuccess) {
-            set_error("cudaStreamEndCapture", e);
-            return FG_E_CUDA;
+    cudaEvent_t ev[6];
+    for (int k = 0; k < 2 * nc; k++) cudaEventCreate(&ev[k]);
+    for (int c = 0; c < nc; c++) {
+        set_kernel(cands[c]);
+        cudaGraphExec_t ge = nullptr;
+        if (use_graphs) {
+            int r = graph_for_current(&ge);
+            if (r != FG_OK) return r;
         }
-        CK(cudaGraphInstantiate(&graph_exec, graph, 0));
-        graph_stages = stages;
-        graph_fused = fused_integrate;
-        graph_digits = digit_bits;
+        cudaEventRecord(ev[2 * c], stream);
+        if (use_graphs) CK(cudaGraphLaunch(ge, stream));
+        else enqueue_step();
+        cudaEventRecord(ev[2 * c + 1], stream);
+        tune_count[cands[c]]++;
+        counted_steps++;
+        step_count++;
     }
-    for (uint32_t k = 0; k < nsteps; k++) CK(cudaGraphLaunch(graph_exec, stream));
+    CK(cudaStreamSynchronize(stream));
+    int best = cands[0];
+    float best_ms = 1e30f;
+    for (int c = 0; c < nc; c++) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[2 * c], ev[2 * c + 1]);
+        tune_last_ms[cands[c]] = ms;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = cands[c];
+        }
+    }
+    for (int k = 0; k < 2 * nc; k++) cudaEventDestroy(ev[k]);
+    set_kernel(best);
+    *done = (uint32_t)nc;
+    return FG_OK;
+}
+
+int World::step(uint32_t nsteps)
+{
+    for (uint32_t k = 0; k < nsteps; k++) {
+        if (tune_period && !use_order && (step_count % tune_period == 0) && nsteps - k >= 3) {
+            uint32_t done = 0;
+            int r = tune_steps(&done);
+            if (r != FG_OK) return r;
+            if (done) {
+                k += done - 1;
+                continue;
+            }
+        }
+        const bool refresh = use_order && !use_cc && (stages & FG_STAGE_DENSITY) &&
+                             (!order_valid || (order_period && step_count % order_period == 0));
+        if (refresh) enqueue_order_refresh();
+        if (!use_graphs) {
+            enqueue_step();
+        } else {
+            cudaGraphExec_t ge = nullptr;
+            int r = graph_for_current(&ge);
+            if (r != FG_OK) return r;
+            CK(cudaGraphLaunch(ge, stream));
+        }
+        tune_count[current_kernel()]++;
+        counted_steps++;
+        step_count++;
+    }
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess) {
+        set_error("step", e);
+        return FG_E_CUDA;
+    }
     return FG_OK;
 }
 
@@ -594,7 +718,11 @@ int World::stage_profile(size_t fbytes, float *ms)
         launch_fill(flush_buf, fbytes / 4, 7u, stream);
     }
     for (int k = 0; k < 8; k++) ms[k] = 0.0f;
+    if (use_order && !order_valid) enqueue_order_refresh();
     enqueue_step(E.ev.data());
+    step_count++;
+    counted_steps++;
+    tune_count[current_kernel()]++;
     CK(cudaStreamSynchronize(stream));
     for (int k = 0; k < 8; k++) {
         if (cudaEventQuery(E.ev[2 * k]) != cudaSuccess || cudaEventQuery(E.ev[2 * k + 1]) != cudaSuccess) {
@@ -936,6 +1064,80 @@ int fg_world_set_graphs(fg_world *w, int on)
     if (!w) return FG_E_INVALID;
     ((World *)w)->use_graphs = on != 0;
     return FG_OK;
+}
+
+int fg_world_set_option(fg_world *w, int option, int value)
+{
+    if (!w) return FG_E_INVALID;
+    World *W = (World *)w;
+    switch (option) {
+    case FG_OPT_NEIGHBOR_LIST: W->use_list = value != 0; return FG_OK;
+    case FG_OPT_TARGET_ORDER: W->use_order = value != 0; return FG_OK;
+    case FG_OPT_ORDER_PERIOD:
+        if (value < 0) return FG_E_INVALID;
+        W->order_period = (uint32_t)value;
+        return FG_OK;
+    case FG_OPT_DIGIT_BITS:
+        if (value < 1 || value > 8) return FG_E_INVALID;
+        W->digit_bits = (uint32_t)value;
+        return FG_OK;
+    case FG_OPT_KERNEL:
+        if (value < 0 || value > 2) return FG_E_INVALID;
+        W->set_kernel(value);
+        return FG_OK;
+    case FG_OPT_AUTOTUNE_PERIOD:
+        if (value < 0) return FG_E_INVALID;
+        W->tune_period = (uint32_t)value;
+        return FG_OK;
+    case FG_OPT_AUTOTUNE_KERNELS:
+        if (value <= 0 || value > 7) return FG_E_INVALID;
+        W->tune_kernels = (uint32_t)value;
+        return FG_OK;
+    default: return FG_E_INVALID;
+    }
+}
+
+int fg_world_counters(fg_world *w, int reset, uint64_t *pair_visits, uint64_t *steps)
+{
+    if (!w) return FG_E_INVALID;
+    World *W = (World *)w;
+    CK(cudaStreamSynchronize(W->stream));
+    unsigned long long v = 0;
+    CK(cudaMemcpy(&v, W->pair_counter, sizeof(v), cudaMemcpyDeviceToHost));
+    if (pair_visits) *pair_visits = v;
+    if (steps) *steps = W->counted_steps;
+    if (reset) {
+        CK(cudaMemset(W->pair_counter, 0, sizeof(v)));
+        W->counted_steps = 0;
+    }
+    return FG_OK;
+}
+
+int fg_world_tuning_stats(const fg_world *w, uint32_t steps_per_kernel[3], float last_trial_ms[3])
+{
+    if (!w) return FG_E_INVALID;
+    const World *W = (const World *)w;
+    for (int k = 0; k < 3; k++) {
+        if (steps_per_kernel) steps_per_kernel[k] = W->tune_count[k];
+        if (last_trial_ms) last_trial_ms[k] = W->tune_last_ms[k];
+    }
+    return FG_OK;
+}
+
+int fg_world_get_option(const fg_world *w, int option, int *value)
+{
+    if (!w || !value) return FG_E_INVALID;
+    const World *W = (const World *)w;
+    switch (option) {
+    case FG_OPT_NEIGHBOR_LIST: *value = W->use_list ? 1 : 0; return FG_OK;
+    case FG_OPT_TARGET_ORDER: *value = W->use_order ? 1 : 0; return FG_OK;
+    case FG_OPT_ORDER_PERIOD: *value = (int)W->order_period; return FG_OK;
+    case FG_OPT_DIGIT_BITS: *value = (int)W->digit_bits; return FG_OK;
+    case FG_OPT_KERNEL: *value = W->current_kernel(); return FG_OK;
+    case FG_OPT_AUTOTUNE_PERIOD: *value = (int)W->tune_period; return FG_OK;
+    case FG_OPT_AUTOTUNE_KERNELS: *value = (int)W->tune_kernels; return FG_OK;
+    default: return FG_E_INVALID;
+    }
 }
 
 uint32_t fg_world_launches_per_step(const fg_world *w)

@@ -33,6 +33,20 @@ struct World {
     uint32_t *keys_u = nullptr, *keys = nullptr, *ids = nullptr, *start = nullptr, *end = nullptr;
     RadixScratch rs{nullptr, nullptr, nullptr};
     NbrList nbr{nullptr, nullptr, nullptr, 0}; /* density -> forces neighbour lists */
+    uint32_t *inv = nullptr;  /* particle -> sorted index (written by the ranges pass) */
+    uint32_t *tord = nullptr; /* spatial target order (particle ids, scene-contiguous) */
+    bool use_list = true, use_order = false;
+    bool use_cc = false;       /* cell-cooperative density/forces (warp per bucket run) */
+    uint32_t *runs = nullptr;  /* occupied-bucket run heads */
+    uint32_t *nruns = nullptr; /* device counter */
+    uint32_t order_period = 16, order_bits = 8, order_scene_shift = 24, order_key_bits = 24;
+    uint64_t step_count = 0;
+    bool order_valid = false;
+    void enqueue_order_refresh();
+    TargetOrder target_order() const
+    {
+        return (use_order && order_valid) ? TargetOrder{tord, inv} : TargetOrder{nullptr, nullptr};
+    }
     /* rigid */
     float4 *rb_local = nullptr, *rb_world = nullptr, *rb_spos = nullptr, *rb_force = nullptr, *rb_torque = nullptr;
     uint32_t *rb_keys_u = nullptr, *rb_keys = nullptr, *rb_ids = nullptr, *rb_start = nullptr, *rb_end = nullptr;
@@ -42,16 +56,36 @@ struct World {
     double *bmass = nullptr, *binv = nullptr;
     uint32_t *body_scene = nullptr, *body_first = nullptr, *body_count = nullptr;
     uint32_t *status_d = nullptr;
+    unsigned long long *pair_counter = nullptr; /* in-range pair visits since the last reset */
+    uint64_t counted_steps = 0;
     /* execution */
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     uint32_t stages = 255;
     bool fused_integrate = true;
     bool use_graphs = true;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t graph_exec = nullptr;
-    uint32_t graph_stages = 0, graph_digits = 0;
-    bool graph_fused = true;
+    /* one instantiated step graph per configuration signature */
+    struct CachedGraph {
+        uint32_t sig;
+        cudaGraph_t graph;
+        cudaGraphExec_t exec;
+    };
+    std::vector<CachedGraph> graphs;
+    uint32_t graph_signature() const;
+    int graph_for_current(cudaGraphExec_t *out);
+    /* online autotuner: every tune_period steps, each candidate kernel runs one
+     * (real) step under CUDA events and the fastest is kept */
+    uint32_t tune_period = 25;
+    uint32_t tune_count[3] = {0, 0, 0}; /* steps run with kernel 0/1/2 */
+    float tune_last_ms[3] = {0.f, 0.f, 0.f};
+    uint32_t tune_kernels = 0x3; /* candidate kernels bit mask */
+    int current_kernel() const { return use_cc ? 2 : (use_list ? 1 : 0); }
+    void set_kernel(int k)
+    {
+        use_cc = (k == 2);
+        use_list = (k == 1);
+    }
+    int tune_steps(uint32_t *done);
     std::vector<void *> allocs;
     size_t device_bytes = 0;
 

@@ -363,27 +363,95 @@ __global__ void __launch_bounds__(256) k_cell_ranges(const uint32_t *__restrict_
                                                     const uint32_t *__restrict__ ids,
                                                     const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                                                     uint32_t *__restrict__ start, uint32_t *__restrict__ end,
-                                                    float4 *__restrict__ spos, float4 *__restrict__ svel, uint32_t n)
+                                                    float4 *__restrict__ spos, float4 *__restrict__ svel, uint32_t n,
+                                                    uint32_t *__restrict__ inv, uint32_t *__restrict__ runs,
+                                                    uint32_t *__restrict__ nruns)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t k = __ldg(keys + i);
         uint32_t prev = i > 0 ? __ldg(keys + i - 1) : k;
-        if (i == 0 || k != prev) {
+        const bool head = (i == 0 || k != prev);
+        if (head) {
             start[k] = i;
             if (i > 0) end[prev] = i;
+        }
+        if (runs) {
+            /* append run heads, one atomic per warp */
+            const uint32_t act = __activemask();
+            const uint32_t m = __ballot_sync(act, head);
+            const int lane = threadIdx.x & 31;
+            const int leader = __ffs(act) - 1;
+            uint32_t base = 0;
+            if (lane == leader && m) base = atomicAdd(nruns, (uint32_t)__popc(m));
+            base = __shfl_sync(act, base, leader);
+            if (head) runs[base + __popc(m & ((1u << lane) - 1u))] = i;
         }
         if (i == n - 1) end[k] = n;
         uint32_t id = __ldg(ids + i);
         spos[i] = __ldg(pos + id);
         if (vel) svel[i] = __ldg(vel + id);
+        if (inv) inv[id] = i; /* particle -> sorted index */
     }
 }
 
 void launch_cell_ranges(const uint32_t *keys, const uint32_t *ids, const float4 *pos, const float4 *vel,
-                        uint32_t *start, uint32_t *end, float4 *spos, float4 *svel, uint32_t n, cudaStream_t st)
+                        uint32_t *start, uint32_t *end, float4 *spos, float4 *svel, uint32_t n, cudaStream_t st,
+                        uint32_t *inv, uint32_t *runs, uint32_t *nruns)
 {
     if (!n) return;
-    k_cell_ranges<<<grid_for((n + 255) / 256, 8), 256, 0, st>>>(keys, ids, pos, vel, start, end, spos, svel, n);
+    k_cell_ranges<<<grid_for((n + 255) / 256, 8), 256, 0, st>>>(keys, ids, pos, vel, start, end, spos, svel, n,
+                                                                inv, runs, nruns);
+}
+
+/* ------------------------------------------------ spatial target order
+ * Density and force kernels process their targets in a spatially coherent
+ * order so that a CTA's particles share neighbour cells and the neighbour
+ * loads hit L1 (the hashed bucket order scatters a CTA over random cells).
+ * The key is the scene id above a Morton code of the particle's cell,
+ * counted from the scene's volume_min and clamped to 2^bits cells per axis;
+ * a particle outside that range only loses locality, never correctness. */
+__device__ __forceinline__ uint32_t fg_spread3(uint32_t v)
+{
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__global__ void __launch_bounds__(FG_CHUNK) k_morton_keys(const FgWork *__restrict__ work, uint32_t nwork,
+                                                         uint32_t n_single, const FgScene *__restrict__ table,
+                                                         const __grid_constant__ FgScene single,
+                                                         const float4 *__restrict__ pos, uint32_t *__restrict__ keys,
+                                                         uint32_t bits, uint32_t scene_shift)
+{
+    const int lim = (1 << bits) - 1;
+    for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+        FgWork it = fg_work(work, w, n_single);
+        if (threadIdx.x >= it.count) continue;
+        const FgScene *S = fg_scene(table, &single, it.scene);
+        const uint32_t t = it.first + threadIdx.x;
+        const float4 p = __ldg(pos + t);
+        int c[3];
+        const float q[3] = {p.x, p.y, p.z};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            float f = (q[a] - S->vmin[a]) / S->cell[a] + 2.0f;
+            int v = (f > 0.0f) ? (int)fminf(f, (float)lim) : 0;
+            c[a] = v > lim ? lim : v;
+        }
+        const uint32_t m = (fg_spread3((uint32_t)c[0]) | (fg_spread3((uint32_t)c[1]) << 1) |
+                            (fg_spread3((uint32_t)c[2]) << 2));
+        keys[t] = (scene_shift < 32 ? (it.scene << scene_shift) : 0u) | m;
+    }
+}
+
+void launch_morton_keys(const Launch &L, const float4 *pos, uint32_t *keys, uint32_t bits, uint32_t scene_shift)
+{
+    if (!L.nwork) return;
+    k_morton_keys<<<grid_for(L.nwork, 16), FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, pos,
+                                                                    keys, bits, scene_shift);
 }
 
 __global__ void k_fill(uint32_t *buf, size_t words, uint32_t v)

@@ -41,9 +41,26 @@ int radix_passes(uint32_t bits, uint32_t digit_bits);
 void radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
                 uint32_t n, uint32_t bits, uint32_t digit_bits, const RadixScratch &s, cudaStream_t st);
 
-/* start[] must be pre-filled with 0xffffffff over the bucket range. */
+/* start[] must be pre-filled with 0xffffffff over the bucket range.
+ * inv (optional) receives particle -> sorted index; runs (optional) receives
+ * the first sorted index of every occupied bucket, in no particular order,
+ * counted in *nruns (zeroed by the caller). */
 void launch_cell_ranges(const uint32_t *keys, const uint32_t *ids, const float4 *pos, const float4 *vel,
-                        uint32_t *start, uint32_t *end, float4 *spos, float4 *svel, uint32_t n, cudaStream_t st);
+                        uint32_t *start, uint32_t *end, float4 *spos, float4 *svel, uint32_t n, cudaStream_t st,
+                        uint32_t *inv = nullptr, uint32_t *runs = nullptr, uint32_t *nruns = nullptr);
+
+/* Spatial (Morton) keys of the unsorted particles: scene id << scene_shift |
+ * Morton code of the cell with `bits` bits per axis (bits <= 10). */
+void launch_morton_keys(const Launch &L, const float4 *pos, uint32_t *keys, uint32_t bits, uint32_t scene_shift);
+
+
+/* Target order of the density/force passes: target slot t processes the
+ * particle tord[t] (a particle id, scene-contiguous), found in sorted order
+ * at inv[tord[t]].  tord == nullptr: slot t is sorted index t. */
+struct TargetOrder {
+    const uint32_t *tord;
+    const uint32_t *inv;
+};
 
 /* ---- SPH (fg_sph.cu) ---- */
 
@@ -53,7 +70,7 @@ void launch_cell_ranges(const uint32_t *keys, const uint32_t *ids, const float4 
  * in-range bucket visits (may exceed FG_NBR_MAX, then forces re-walk the
  * buckets).  rec[2i] = (x, y, z, rho_i), rec[2i+1] = (vx, vy, vz, P_i): one
  * 32-byte sector per neighbour gather. */
-#define FG_NBR_MAX 64u
+#define FG_NBR_MAX 96u
 struct NbrList {
     uint32_t *idx;
     uint32_t *cnt;
@@ -63,7 +80,8 @@ struct NbrList {
 
 void launch_density(const Launch &L, const float4 *spos, const uint32_t *start, const uint32_t *end, float2 *dp,
                     float gas_override, float rest_override, float mass_override, int use_override,
-                    const float4 *svel = nullptr, const NbrList *list = nullptr);
+                    const float4 *svel = nullptr, const NbrList *list = nullptr,
+                    TargetOrder ord = TargetOrder{nullptr, nullptr}, unsigned long long *pairs = nullptr);
 
 struct RigidGrid {
     const float4 *spos;     /* sorted sphere positions, w = body index */
@@ -83,9 +101,21 @@ struct ForceOut {
 void launch_forces(const Launch &L, const float4 *spos, const float4 *svel, const float2 *dp, const uint32_t *start,
                    const uint32_t *end, const uint32_t *ids, ForceOut out, const RigidGrid *rigid,
                    const RigidGrid *statics, float mass_override, float visc_override, int use_override,
-                   const NbrList *list = nullptr);
+                   const NbrList *list = nullptr, TargetOrder ord = TargetOrder{nullptr, nullptr});
 
 void launch_integrate(const Launch &L, float4 *pos, const float4 *vel);
+
+/* ---- cell-cooperative density/forces (fg_sph_cc.cu): one warp per bucket
+ * run, neighbour candidates staged in shared memory.  rec receives / holds
+ * the packed per-particle records (x, y, z, rho), (vx, vy, vz, P). */
+void launch_density_cc(const FgScene *table, const FgScene *single, uint32_t nscenes, const uint32_t *runs,
+                       const uint32_t *nruns, const uint32_t *keys, const float4 *spos, const float4 *svel,
+                       const uint32_t *start, const uint32_t *end, float2 *dp, float4 *rec, uint32_t n,
+                       cudaStream_t s);
+void launch_forces_cc(const FgScene *table, const FgScene *single, uint32_t nscenes, const uint32_t *runs,
+                      const uint32_t *nruns, const uint32_t *keys, const float4 *spos, const float4 *svel,
+                      const float4 *rec, const uint32_t *start, const uint32_t *end, const uint32_t *ids,
+                      ForceOut out, const RigidGrid *rigid, uint32_t n, cudaStream_t s);
 
 /* ---- rigid bodies (fg_rigid.cu) ---- */
 void launch_rb_from_fluid(const Launch &Lrb, const float4 *rb_spos, const uint32_t *rb_ids, const float4 *body_vel,

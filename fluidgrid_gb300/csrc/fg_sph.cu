@@ -29,6 +29,7 @@
 #include <string.h>
 #include "fg_device.cuh"
 #include "fg_kernels.h"
+#include "fg_sph_common.cuh"
 
 namespace fg {
 
@@ -46,7 +47,9 @@ struct Kahan {
 
 /* Visit the particles of the 27 neighbour buckets in the reference's order
  * (z outer, x inner, each from -1 to 1; ascending sorted index inside a
- * bucket).  Fully unrolled so the per-axis hashes live in registers. */
+ * bucket).  One runtime loop over the 27 buckets with the per-axis hashes
+ * selected from registers: compact code (an unrolled walk multiplies the
+ * body 27 times and thrashes the instruction cache) and no local memory. */
 template <typename Fn>
 __device__ __forceinline__ void fg_walk27(float px, float py, float pz, const FgScene *S,
                                           const uint32_t *__restrict__ start, const uint32_t *__restrict__ end,
@@ -54,19 +57,19 @@ __device__ __forceinline__ void fg_walk27(float px, float py, float pz, const Fg
 {
     uint32_t hx[3], hy[3], hz[3];
     fg_neighbour_hashes(px, py, pz, S->cell, hx, hy, hz);
+    const uint32_t hx0 = hx[0], hx1 = hx[1], hx2 = hx[2], hy0 = hy[0], hy1 = hy[1], hy2 = hy[2];
+    const uint32_t hz0 = hz[0], hz1 = hz[1], hz2 = hz[2];
     const uint32_t nb = S->nb, mask = S->nb_mask, bb = S->bucket_base;
-#pragma unroll
-    for (int z = 0; z < 3; z++)
-#pragma unroll
-        for (int y = 0; y < 3; y++)
-#pragma unroll
-            for (int x = 0; x < 3; x++) {
-                const uint32_t b = bb + fg_bucket(hx[x], hy[y], hz[z], nb, mask);
-                const uint32_t st = __ldg(start + b);
-                if (st == FG_EMPTY) continue;
-                const uint32_t en = __ldg(end + b);
-                for (uint32_t j = st; j < en; j++) fn(j);
-            }
+#pragma unroll 1
+    for (int k = 0; k < 27; k++) {
+        const int z = k / 9, y = (k / 3) % 3, x = k % 3;
+        const uint32_t b = bb + fg_bucket(fg_sel3(hx0, hx1, hx2, x), fg_sel3(hy0, hy1, hy2, y),
+                                          fg_sel3(hz0, hz1, hz2, z), nb, mask);
+        const uint32_t st = __ldg(start + b);
+        if (st == FG_EMPTY) continue;
+        const uint32_t en = __ldg(end + b);
+        for (uint32_t j = st; j < en; j++) fn(j);
+    }
 }
 
 template <bool LIST>
@@ -78,15 +81,16 @@ __global__ void __launch_bounds__(FG_CHUNK) k_density(const FgWork *__restrict__
                                                      const uint32_t *__restrict__ start,
                                                      const uint32_t *__restrict__ end, float2 *__restrict__ dp,
                                                      float gas_o, float rest_o, float mass_o, int use_o,
-                                                     const __grid_constant__ NbrList list)
+                                                     const __grid_constant__ NbrList list, TargetOrder ord,
+                                                     unsigned long long *__restrict__ pairs)
 {
-    __shared__ uint32_t s_nbr[LIST ? FG_NBR_MAX : 1][FG_CHUNK];
     const uint32_t tid = threadIdx.x;
     for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
         FgWork it = fg_work(work, w, n_single);
         const bool valid = tid < it.count;
         const FgScene *S = fg_scene(table, &single, it.scene);
-        const uint32_t i = it.first + tid;
+        const uint32_t tpos = it.first + tid; /* target slot */
+        const uint32_t i = (ord.tord && valid) ? __ldg(ord.inv + __ldg(ord.tord + tpos)) : tpos;
         const float4 p = valid ? spos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const bool active = valid && p.w > 0.0f; /* inactive: density not written */
         uint32_t cnt = 0;
@@ -101,10 +105,11 @@ __global__ void __launch_bounds__(FG_CHUNK) k_density(const FgWork *__restrict__
                 if (r2 < h2) {
                     const float t = h2 - r2;
                     acc.add(t * t * t);
-                    if (LIST) {
-                        if (cnt < FG_NBR_MAX) s_nbr[cnt][tid] = j;
-                        cnt++;
-                    }
+                    /* straight to the SoA slot: the L2 merges the partial
+                     * sector writes, no shared-memory staging (which would
+                     * cost occupancy and L1 capacity) */
+                    if (LIST && cnt < FG_NBR_MAX) list.idx[(size_t)cnt * list.stride + tpos] = j;
+                    cnt++;
                 }
             });
             const float mass = use_o ? mass_o : S->mass;
@@ -125,72 +130,30 @@ __global__ void __launch_bounds__(FG_CHUNK) k_density(const FgWork *__restrict__
             list.rec[2 * i] = make_float4(p.x, p.y, p.z, d.x);
             list.rec[2 * i + 1] = make_float4(v.x, v.y, v.z, d.y);
         }
-        if (LIST) {
-            if (valid) list.cnt[i] = cnt;
-            const uint32_t m = cnt < FG_NBR_MAX ? cnt : FG_NBR_MAX;
-            const uint32_t wm = __reduce_max_sync(0xffffffffu, m);
-            for (uint32_t k = 0; k < wm; k++)
-                if (k < m) list.idx[(size_t)k * list.stride + i] = s_nbr[k][tid];
+        if (LIST && valid) list.cnt[tpos] = cnt;
+        if (pairs) {
+            /* in-range pair visits of this warp (self included), for reporting */
+            const uint32_t s = __reduce_add_sync(0xffffffffu, cnt);
+            if ((tid & 31) == 0 && s) atomicAdd(pairs, (unsigned long long)s);
         }
     }
 }
 
 void launch_density(const Launch &L, const float4 *spos, const uint32_t *start, const uint32_t *end, float2 *dp,
-                    float gas_o, float rest_o, float mass_o, int use_o, const float4 *svel, const NbrList *list)
+                    float gas_o, float rest_o, float mass_o, int use_o, const float4 *svel, const NbrList *list,
+                    TargetOrder ord, unsigned long long *pairs)
 {
     if (!L.nwork) return;
     const uint32_t g = grid_for(L.nwork, 16);
     if (list) {
         k_density<true><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, start,
-                                                      end, dp, gas_o, rest_o, mass_o, use_o, *list);
+                                                      end, dp, gas_o, rest_o, mass_o, use_o, *list, ord, pairs);
     } else {
         NbrList none;
         memset(&none, 0, sizeof(none));
         k_density<false><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, start,
-                                                       end, dp, gas_o, rest_o, mass_o, use_o, none);
+                                                       end, dp, gas_o, rest_o, mass_o, use_o, none, ord, pairs);
     }
-}
-
-/* Rigid-sphere contact of one fluid particle against a rigid grid
- * (ProcessCollisionForcesD with the per-body velocity of w, eps from the
- * scene).  Skipped when the particle is outside the scene's sphere AABB
- * grown by the contact distance: there every candidate is out of range, so
- * the sum is exactly zero as in the reference. */
-__device__ __forceinline__ float3 fg_fluid_rigid_contact(const FgScene *S, uint32_t scene, float4 p, float4 v,
-                                                         const RigidGrid &G, bool dynamic)
-{
-    float3 acc = make_float3(0.f, 0.f, 0.f);
-    const float mind = S->fluid_radius + S->rb_radius + S->fluid_eps;
-    if (G.aabb) {
-        const int *bx = G.aabb + 6 * scene;
-        if (p.x < fg_ord_float(bx[0]) - mind || p.y < fg_ord_float(bx[1]) - mind ||
-            p.z < fg_ord_float(bx[2]) - mind || p.x > fg_ord_float(bx[3]) + mind ||
-            p.y > fg_ord_float(bx[4]) + mind || p.z > fg_ord_float(bx[5]) + mind)
-            return acc;
-    }
-    const float3 P = make_float3(p.x, p.y, p.z);
-    const float3 V = make_float3(v.x, v.y, v.z);
-    const int rx = S->f2r_rel[0], ry = S->f2r_rel[1], rz = S->f2r_rel[2];
-    for (int z = -rz; z <= rz; z++) {
-        const uint32_t hz = fg_axis_hash_rel(p.z, S->rb_cell[2], z, FG_PZ);
-        for (int y = -ry; y <= ry; y++) {
-            const uint32_t hy = fg_axis_hash_rel(p.y, S->rb_cell[1], y, FG_PY);
-            for (int x = -rx; x <= rx; x++) {
-                const uint32_t hx = fg_axis_hash_rel(p.x, S->rb_cell[0], x, FG_PX);
-                const uint32_t b = G.own_geometry ? fg_bucket(hx, hy, hz, G.nb, G.mask)
-                                                  : S->rb_bucket_base + fg_bucket(hx, hy, hz, S->rb_nb, S->rb_nb_mask);
-                const uint32_t st = __ldg(G.start + b);
-                if (st == FG_EMPTY) continue;
-                const uint32_t en = __ldg(G.end + b);
-                for (uint32_t j = st; j < en; j++) {
-                    const float4 q = __ldg(G.spos + j);
-                    const float4 vq = dynamic ? __ldg(G.body_vel + (int)q.w) : make_float4(0.f, 0.f, 0.f, 0.f);
-                    fg_contact(acc, P, V, q, vq, mind, S->ck, S->ckd);
-                }
-            }
-        }
-    }
-    return acc;
 }
 
 struct RigidArgs {
@@ -198,25 +161,6 @@ struct RigidArgs {
     RigidGrid sta;
     int use_dyn, use_sta;
 };
-
-/* Pressure + viscosity of neighbour j on i (SPHCalculatePressureForceD +
- * SPHCalculateViscosityForceD): d = p_i - p_j (scaled), r2 = |d|^2 <= h^2. */
-__device__ __forceinline__ void fg_pair(float &fx, float &fy, float &fz, float dx, float dy, float dz, float r2,
-                                        float h, float kspiky, float kv, float rho_i, float P_i, float4 vi,
-                                        float rho_j, float P_j, float4 vj)
-{
-    const float il = rsqrtf(r2);
-    const float l = r2 * il;
-    const float hl = h - l;
-    const float irr = __frcp_rn(rho_i * rho_j);
-    /* pressure: -(d/l) kSpiky (h-l)^2 (Pi+Pj)/(rho_i rho_j) */
-    const float cp = -(kspiky * hl * hl) * ((P_i + P_j) * irr) * il;
-    /* viscosity: (vj-vi)/(rho_i rho_j) kVisc (h-l) mu */
-    const float cv = (kv * hl) * irr;
-    fx += dx * cp + (vj.x - vi.x) * cv;
-    fy += dy * cp + (vj.y - vi.y) * cv;
-    fz += dz * cp + (vj.z - vi.z) * cv;
-}
 
 template <bool LIST>
 __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ work, uint32_t nwork,
@@ -229,13 +173,15 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                                                     const uint32_t *__restrict__ ids, float4 *__restrict__ vel_out,
                                                     float4 *__restrict__ pos_out,
                                                     const __grid_constant__ RigidArgs R, float mass_o, float visc_o,
-                                                    int use_o, const __grid_constant__ NbrList list)
+                                                    int use_o, const __grid_constant__ NbrList list, TargetOrder ord)
 {
     for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
         FgWork it = fg_work(work, w, n_single);
         if (threadIdx.x >= it.count) continue;
         const FgScene *S = fg_scene(table, &single, it.scene);
-        const uint32_t i = it.first + threadIdx.x;
+        const uint32_t tpos = it.first + threadIdx.x; /* target slot */
+        const uint32_t pid = ord.tord ? __ldg(ord.tord + tpos) : 0u;
+        const uint32_t i = ord.tord ? __ldg(ord.inv + pid) : tpos;
         const float4 p = spos[i];
         const float4 v = svel[i];
         float3 F = make_float3(0.f, 0.f, 0.f);
@@ -249,9 +195,10 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
             if (LIST) {
                 const float4 r0 = list.rec[2 * i], r1 = list.rec[2 * i + 1];
                 const float rho_i = r0.w, P_i = r1.w;
-                const uint32_t c = list.cnt[i];
+                const uint32_t c = list.cnt[tpos];
                 if (c <= FG_NBR_MAX) {
-                    const uint32_t *nl = list.idx + i;
+                    const uint32_t *nl = list.idx + tpos;
+#pragma unroll 2
                     for (uint32_t k = 0; k < c; k++) {
                         const uint32_t j = __ldg(nl + (size_t)k * list.stride);
                         if (j == i) continue;
@@ -313,7 +260,7 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
         nv.y = v.y + F.y * dt;
         nv.z = v.z + F.z * dt;
         nv.w = v.w + 0.0f;
-        const uint32_t oi = __ldg(ids + i);
+        const uint32_t oi = ord.tord ? pid : __ldg(ids + i);
         vel_out[oi] = nv;
         if (pos_out && p.w > 0.0f) {
             /* SPHIntegrateK fused: pos += vel * (dt / scale), unfused rounding */
@@ -330,7 +277,8 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
 
 void launch_forces(const Launch &L, const float4 *spos, const float4 *svel, const float2 *dp, const uint32_t *start,
                    const uint32_t *end, const uint32_t *ids, ForceOut out, const RigidGrid *rigid,
-                   const RigidGrid *statics, float mass_o, float visc_o, int use_o, const NbrList *list)
+                   const RigidGrid *statics, float mass_o, float visc_o, int use_o, const NbrList *list,
+                   TargetOrder ord)
 {
     if (!L.nwork) return;
     RigidArgs R;
@@ -340,13 +288,13 @@ void launch_forces(const Launch &L, const float4 *spos, const float4 *svel, cons
     const uint32_t g = grid_for(L.nwork, 16);
     if (list) {
         k_forces<true><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, dp, start,
-                                                     end, ids, out.vel, out.pos, R, mass_o, visc_o, use_o, *list);
+                                                     end, ids, out.vel, out.pos, R, mass_o, visc_o, use_o, *list, ord);
     } else {
         NbrList none;
         memset(&none, 0, sizeof(none));
         k_forces<false><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, dp,
                                                       start, end, ids, out.vel, out.pos, R, mass_o, visc_o, use_o,
-                                                      none);
+                                                      none, ord);
     }
 }
 

@@ -109,6 +109,32 @@ class World:
     def set_graphs(self, on):
         check(self.L.fg_world_set_graphs(self.h, 1 if on else 0), "set_graphs")
 
+    def set_option(self, name, value):
+        check(self.L.fg_world_set_option(self.h, _ffi.OPTIONS[name], int(value)), "fg_world_set_option")
+
+    def get_option(self, name):
+        v = ctypes.c_int()
+        check(self.L.fg_world_get_option(self.h, _ffi.OPTIONS[name], ctypes.byref(v)), "fg_world_get_option")
+        return int(v.value)
+
+    def options(self):
+        return {k: self.get_option(k) for k in _ffi.OPTIONS}
+
+    def counters(self, reset=False):
+        """(in-range pair visits, steps) counted since the last reset."""
+        pv = ctypes.c_uint64()
+        st = ctypes.c_uint64()
+        check(self.L.fg_world_counters(self.h, 1 if reset else 0, ctypes.byref(pv), ctypes.byref(st)),
+              "fg_world_counters")
+        return int(pv.value), int(st.value)
+
+    def tuning_stats(self):
+        """Steps run with each density/force kernel and the last trial times."""
+        cnt = (ctypes.c_uint32 * 3)()
+        ms = (ctypes.c_float * 3)()
+        check(self.L.fg_world_tuning_stats(self.h, cnt, ms), "fg_world_tuning_stats")
+        return {"steps_per_kernel": list(cnt), "last_trial_ms": [round(x, 4) for x in ms]}
+
     def launches_per_step(self):
         return int(self.L.fg_world_launches_per_step(self.h))
 
