@@ -244,6 +244,7 @@ def run_ours(args, rank, world, local):
     pair_visits, counted = w.counters(reset=True)
     w.check_finite()
     tuning = w.tuning_stats()
+    tuning["list_overflow_particle_steps"] = w.list_overflows(reset=True)
     w.close()
     # 2. end to end on the same trajectory: every step uploads the particle
     #    state from pinned host memory and downloads it again (the download of

@@ -76,7 +76,9 @@ STAGE_RB_GRID, STAGE_RB_CONTACT, STAGE_FORCES, STAGE_BODIES = 16, 32, 64, 128
 STAGE_ALL = 255
 
 OPTIONS = {"neighbor_list": 1, "target_order": 2, "order_period": 3, "digit_bits": 4, "kernel": 5,
-           "autotune_period": 6, "autotune_kernels": 7}
+           "autotune_period": 6, "autotune_kernels": 7, "list_cap": 8, "ctas_per_sm": 10,
+           "autotune_tiles": 11, "list_autogrow": 12}
+NUM_KERNELS = 3
 
 STATUS = {0: "FG_OK", 1: "FG_E_INVALID", 2: "FG_E_CUDA", 3: "FG_E_OOM", 4: "FG_E_BUDGET", 5: "FG_E_NONFINITE",
           6: "FG_E_TIMEOUT", 7: "FG_E_STATE", 8: "FG_E_UNSUPPORTED", 9: "FG_E_NOLIB"}
@@ -90,7 +92,7 @@ C_ABI_SYMBOLS = [
     "fg_world_set_graphs", "fg_world_launches_per_step", "fg_world_stage_profile", "fg_world_timed_steps",
     "fg_world_e2e_steps", "fg_host_alloc", "fg_host_free", "fg_set_device", "fg_probe_fp32_peak",
     "fg_sort_pairs_noalloc", "fg_world_set_option", "fg_world_get_option", "fg_world_tuning_stats",
-    "fg_world_counters",
+    "fg_world_counters", "fg_world_list_overflows",
     "fg_memcpy_d2h", "fg_memcpy_h2d",
     "fg_device_synchronize", "fg_last_error", "fg_version"]
 REFERENCE_SYMBOLS = [
@@ -154,6 +156,7 @@ def load():
     L.fg_world_get_option.argtypes = [VP, ctypes.c_int, P(ctypes.c_int)]
     L.fg_world_tuning_stats.argtypes = [VP, P(c_u32), P(c_f)]
     L.fg_world_counters.argtypes = [VP, ctypes.c_int, P(ctypes.c_uint64), P(ctypes.c_uint64)]
+    L.fg_world_list_overflows.argtypes = [VP, ctypes.c_int, P(ctypes.c_uint64)]
     L.fg_memcpy_d2h.argtypes = [VP, VP, ctypes.c_size_t]
     L.fg_memcpy_h2d.argtypes = [VP, VP, ctypes.c_size_t]
     L.fg_last_error.restype = ctypes.c_char_p

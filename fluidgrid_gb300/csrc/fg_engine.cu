@@ -76,6 +76,8 @@ int World::alloc(void **p, size_t bytes)
 World::~World()
 {
     if (flush_buf) cudaFree(flush_buf);
+    for (auto &e : tr.ev)
+        if (e) cudaEventDestroy(e);
     for (auto &g : graphs) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         if (g.graph) cudaGraphDestroy(g.graph);
@@ -264,10 +266,12 @@ int World::create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st)
     if ((r = A((void **)&rs.keys_alt, 4 * M))) return r;
     if ((r = A((void **)&rs.vals_alt, 4 * M))) return r;
     if ((r = A((void **)&rs.hist, 4 * radix_hist_words((uint32_t)M)))) return r;
-    if ((r = A((void **)&nbr.idx, 4 * (size_t)FG_NBR_MAX * N))) return r;
+    list_cap_alloc = FG_LIST_CAP_DEFAULT;
+    if ((r = A((void **)&nbr.idx, 4 * (size_t)list_cap_alloc * N))) return r;
+    nbr.cap = list_cap_alloc;
+    nbr.max_count = nullptr;
     if ((r = A((void **)&nbr.cnt, 4 * N))) return r;
     if ((r = A((void **)&nbr.rec, 32 * N))) return r;
-    nbr.stride = (uint32_t)N;
     if ((r = A((void **)&runs, 4 * N))) return r;
     if ((r = A((void **)&nruns, 16))) return r;
     if ((r = A((void **)&inv, 4 * N))) return r;
@@ -280,8 +284,17 @@ int World::create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st)
     }
     if ((r = A((void **)&status_d, 64))) return r;
     CK(cudaMemsetAsync(status_d, 0, 64, stream));
-    pair_counter = (unsigned long long *)(status_d + 8); /* 8-byte aligned slot of the status block */
+    pair_counter = (unsigned long long *)(status_d + 8); /* 8-byte aligned slots of the status block */
+    overflow_counter = (unsigned long long *)(status_d + 10);
+    max_count = status_d + 12;
+    nbr.max_count = max_count;
+    nbr.overflow = overflow_counter;
     CK(cudaMemsetAsync(dp, 0, 8 * N, stream));
+    /* lists read before any density pass (stage-split calls) see zero
+     * counts and in-range indices */
+    CK(cudaMemsetAsync(nbr.cnt, 0, 4 * N, stream));
+    CK(cudaMemsetAsync(nbr.idx, 0, 4 * (size_t)list_cap_alloc * N, stream));
+    CK(cudaMemsetAsync(nbr.rec, 0, 32 * N, stream));
     CK(cudaMemsetAsync(vel, 0, 16 * N, stream));
     CK(cudaMemsetAsync(end, 0, 4 * (size_t)std::max<uint32_t>(total_buckets, 1), stream));
 
@@ -382,6 +395,7 @@ Launch World::fluid_launch() const
     L.nwork = nwork;
     L.n = n;
     L.stream = stream;
+    L.ctas_per_sm = ctas_per_sm;
     return L;
 }
 
@@ -394,6 +408,7 @@ Launch World::sphere_launch() const
     L.nwork = nwork_sph;
     L.n = nspheres;
     L.stream = stream;
+    L.ctas_per_sm = 0;
     return L;
 }
 
@@ -427,7 +442,7 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
     if (stages & FG_STAGE_RANGES) {
         mark(2, 0);
         cudaMemsetAsync(start, 0xff, 4 * (size_t)total_buckets, stream);
-        if (use_cc) {
+        if (needs_runs()) {
             cudaMemsetAsync(nruns, 0, 4, stream);
             launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv, runs, nruns);
         } else {
@@ -524,15 +539,44 @@ void World::enqueue_order_refresh()
     order_valid = true;
 }
 
-uint32_t World::graph_signature() const
+uint64_t World::graph_signature() const
 {
-    return (stages & 0xffu) | (fused_integrate ? 0x100u : 0u) | (digit_bits << 9) | (use_list ? 0x10000u : 0u) |
-           ((use_order && order_valid) ? 0x20000u : 0u) | (use_cc ? 0x40000u : 0u);
+    return (uint64_t)((stages & 0xffu) | (fused_integrate ? 0x100u : 0u) | (digit_bits << 9) |
+                      (use_list ? 0x10000u : 0u) | ((use_order && order_valid) ? 0x20000u : 0u) |
+                      (use_cc ? 0x40000u : 0u) | ((ctas_per_sm & 0x7fu) << 20)) |
+           ((uint64_t)nbr.cap << 32);
+}
+
+int World::set_list_cap(uint32_t cap)
+{
+    if (cap < 1 || cap > FG_LIST_CAP_MAX) return FG_E_INVALID;
+    cap = (cap + 3u) & ~3u; /* lists are stored four entries at a time */
+    if (cap > list_cap_alloc) {
+        CK(cudaStreamSynchronize(stream));
+        const size_t N = std::max<uint32_t>(n, 1);
+        uint32_t *p = nullptr;
+        CK(cudaMalloc(&p, 4 * (size_t)cap * N));
+        CK(cudaMemsetAsync(p, 0, 4 * (size_t)cap * N, stream));
+        for (auto &a : allocs)
+            if (a == (void *)nbr.idx) a = p;
+        cudaFree(nbr.idx);
+        device_bytes += 4 * (size_t)(cap - list_cap_alloc) * N;
+        nbr.idx = p;
+        list_cap_alloc = cap;
+        /* every captured step holds the old list pointer */
+        for (auto &g : graphs) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            if (g.graph) cudaGraphDestroy(g.graph);
+        }
+        graphs.clear();
+    }
+    nbr.cap = cap;
+    return FG_OK;
 }
 
 int World::graph_for_current(cudaGraphExec_t *out)
 {
-    const uint32_t sig = graph_signature();
+    const uint64_t sig = graph_signature();
     for (auto &g : graphs)
         if (g.sig == sig) {
             *out = g.exec;
@@ -557,67 +601,101 @@ int World::graph_for_current(cudaGraphExec_t *out)
     return FG_OK;
 }
 
-/* One autotuning round: each candidate kernel runs one real step bracketed
- * by events (the state advances as in any step); the fastest is kept. */
-int World::tune_steps(uint32_t *done)
+/* Autotuning round: the candidate values of one tunable (rotating among the
+ * kernel, kernel 3's block warps and the radix digit width) each run one
+ * real step between CUDA events -- the state advances as in any step -- and
+ * the fastest value is kept.  A round may span several step() calls. */
+void World::tune_begin()
 {
-    int cands[3], nc = 0;
-    for (int k = 0; k < 3; k++)
-        if (tune_kernels & (1u << k)) cands[nc++] = k;
-    if (nc < 2) {
-        *done = 0;
-        return FG_OK;
+    int dims[3], nd = 0;
+    if (__builtin_popcount(tune_kernels & 0x7u) >= 2) dims[nd++] = 0;
+    if ((tune_tiles & 1u) && !use_cc) dims[nd++] = 1;
+    if (tune_tiles & 2u) dims[nd++] = 2;
+    tr.ncand = 0;
+    if (!nd) return;
+    tr.dim = dims[tune_round++ % (uint32_t)nd];
+    if (tr.dim == 0) {
+        for (int k = 0; k < 3; k++)
+            if (tune_kernels & (1u << k)) tr.cand[tr.ncand++] = k;
+    } else if (tr.dim == 1) {
+        /* CTAs per SM of the 128-thread density/force grids */
+        const int v[3] = {8, 16, 64};
+        for (int k = 0; k < 3; k++) tr.cand[tr.ncand++] = v[k];
+    } else {
+        for (int v = 6; v <= 8; v++) tr.cand[tr.ncand++] = v;
     }
-    cudaEvent_t ev[6];
-    for (int k = 0; k < 2 * nc; k++) cudaEventCreate(&ev[k]);
-    for (int c = 0; c < nc; c++) {
-        set_kernel(cands[c]);
-        cudaGraphExec_t ge = nullptr;
-        if (use_graphs) {
-            int r = graph_for_current(&ge);
-            if (r != FG_OK) return r;
-        }
-        cudaEventRecord(ev[2 * c], stream);
-        if (use_graphs) CK(cudaGraphLaunch(ge, stream));
-        else enqueue_step();
-        cudaEventRecord(ev[2 * c + 1], stream);
-        tune_count[cands[c]]++;
-        counted_steps++;
-        step_count++;
+    if (tr.ncand < 2) {
+        tr.ncand = 0;
+        return;
     }
-    CK(cudaStreamSynchronize(stream));
-    int best = cands[0];
+    if (!tr.ev[0])
+        for (auto &e : tr.ev)
+            if (cudaEventCreate(&e) != cudaSuccess) {
+                cudaGetLastError();
+                tr.ncand = 0;
+                return;
+            }
+    tr.idx = 0;
+    tr.active = true;
+}
+
+void World::tune_apply(int dim, int v)
+{
+    if (dim == 0) set_kernel(v);
+    else if (dim == 1) ctas_per_sm = (uint32_t)v;
+    else digit_bits = (uint32_t)v;
+}
+
+int World::tune_finish()
+{
+    tr.active = false;
+    CK(cudaEventSynchronize(tr.ev[2 * tr.ncand - 1]));
+    int best = tr.cand[0];
     float best_ms = 1e30f;
-    for (int c = 0; c < nc; c++) {
+    for (int c = 0; c < tr.ncand; c++) {
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, ev[2 * c], ev[2 * c + 1]);
-        tune_last_ms[cands[c]] = ms;
+        CK(cudaEventElapsedTime(&ms, tr.ev[2 * c], tr.ev[2 * c + 1]));
+        if (tr.dim == 0) tune_last_ms[tr.cand[c]] = ms;
         if (ms < best_ms) {
             best_ms = ms;
-            best = cands[c];
+            best = tr.cand[c];
         }
     }
-    for (int k = 0; k < 2 * nc; k++) cudaEventDestroy(ev[k]);
-    set_kernel(best);
-    *done = (uint32_t)nc;
+    tune_apply(tr.dim, best);
     return FG_OK;
+}
+
+/* Every FG_LIST_CHECK_PERIOD steps (kernel 3): grow the neighbour-list
+ * capacity to 1.125x the largest in-range count seen since the last check,
+ * so the force pass walks lists instead of buckets as a scene compresses. */
+int World::check_list_cap()
+{
+    uint32_t mx = 0;
+    CK(cudaMemcpyAsync(&mx, max_count, 4, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaMemsetAsync(max_count, 0, 4, stream));
+    if (mx <= nbr.cap) return FG_OK;
+    const uint32_t want = std::min<uint32_t>(((mx + mx / 8u) + 31u) & ~31u, FG_LIST_CAP_MAX);
+    if (want <= nbr.cap) return FG_OK;
+    return set_list_cap(want);
 }
 
 int World::step(uint32_t nsteps)
 {
     for (uint32_t k = 0; k < nsteps; k++) {
-        if (tune_period && !use_order && (step_count % tune_period == 0) && nsteps - k >= 3) {
-            uint32_t done = 0;
-            int r = tune_steps(&done);
+        if (use_list && list_autogrow && step_count && (step_count % FG_LIST_CHECK_PERIOD == 0)) {
+            int r = check_list_cap();
             if (r != FG_OK) return r;
-            if (done) {
-                k += done - 1;
-                continue;
-            }
         }
-        const bool refresh = use_order && !use_cc && (stages & FG_STAGE_DENSITY) &&
+        if (!tr.active && tune_period && !use_order && (step_count % tune_period == 0)) tune_begin();
+        const bool refresh = use_order && !needs_runs() && (stages & FG_STAGE_DENSITY) &&
                              (!order_valid || (order_period && step_count % order_period == 0));
         if (refresh) enqueue_order_refresh();
+        if (tr.active) {
+            tune_apply(tr.dim, tr.cand[tr.idx]);
+            CK(cudaEventRecord(tr.ev[2 * tr.idx], stream));
+        }
+        const int kused = current_kernel();
         if (!use_graphs) {
             enqueue_step();
         } else {
@@ -626,7 +704,14 @@ int World::step(uint32_t nsteps)
             if (r != FG_OK) return r;
             CK(cudaGraphLaunch(ge, stream));
         }
-        tune_count[current_kernel()]++;
+        if (tr.active) {
+            CK(cudaEventRecord(tr.ev[2 * tr.idx + 1], stream));
+            if (++tr.idx == tr.ncand) {
+                int r = tune_finish();
+                if (r != FG_OK) return r;
+            }
+        }
+        tune_count[kused]++;
         counted_steps++;
         step_count++;
     }
@@ -1093,6 +1178,20 @@ int fg_world_set_option(fg_world *w, int option, int value)
         if (value <= 0 || value > 7) return FG_E_INVALID;
         W->tune_kernels = (uint32_t)value;
         return FG_OK;
+    case FG_OPT_LIST_CAP: {
+        const int r = W->set_list_cap((uint32_t)std::max(value, 0));
+        if (r == FG_OK) W->list_autogrow = false; /* an explicit capacity stays */
+        return r;
+    }
+    case FG_OPT_LIST_AUTOGROW: W->list_autogrow = value != 0; return FG_OK;
+    case FG_OPT_CTAS_PER_SM:
+        if (value < 0 || value > 64) return FG_E_INVALID;
+        W->ctas_per_sm = (uint32_t)value;
+        return FG_OK;
+    case FG_OPT_AUTOTUNE_TILES:
+        if (value < 0 || value > 3) return FG_E_INVALID;
+        W->tune_tiles = (uint32_t)value;
+        return FG_OK;
     default: return FG_E_INVALID;
     }
 }
@@ -1113,11 +1212,24 @@ int fg_world_counters(fg_world *w, int reset, uint64_t *pair_visits, uint64_t *s
     return FG_OK;
 }
 
-int fg_world_tuning_stats(const fg_world *w, uint32_t steps_per_kernel[3], float last_trial_ms[3])
+int fg_world_list_overflows(fg_world *w, int reset, uint64_t *particles)
+{
+    if (!w) return FG_E_INVALID;
+    World *W = (World *)w;
+    CK(cudaStreamSynchronize(W->stream));
+    unsigned long long v = 0;
+    CK(cudaMemcpy(&v, W->overflow_counter, sizeof(v), cudaMemcpyDeviceToHost));
+    if (particles) *particles = v;
+    if (reset) CK(cudaMemset(W->overflow_counter, 0, sizeof(v)));
+    return FG_OK;
+}
+
+int fg_world_tuning_stats(const fg_world *w, uint32_t steps_per_kernel[FG_NUM_KERNELS],
+                          float last_trial_ms[FG_NUM_KERNELS])
 {
     if (!w) return FG_E_INVALID;
     const World *W = (const World *)w;
-    for (int k = 0; k < 3; k++) {
+    for (int k = 0; k < FG_NUM_KERNELS; k++) {
         if (steps_per_kernel) steps_per_kernel[k] = W->tune_count[k];
         if (last_trial_ms) last_trial_ms[k] = W->tune_last_ms[k];
     }
@@ -1136,6 +1248,10 @@ int fg_world_get_option(const fg_world *w, int option, int *value)
     case FG_OPT_KERNEL: *value = W->current_kernel(); return FG_OK;
     case FG_OPT_AUTOTUNE_PERIOD: *value = (int)W->tune_period; return FG_OK;
     case FG_OPT_AUTOTUNE_KERNELS: *value = (int)W->tune_kernels; return FG_OK;
+    case FG_OPT_LIST_CAP: *value = (int)W->nbr.cap; return FG_OK;
+    case FG_OPT_LIST_AUTOGROW: *value = W->list_autogrow ? 1 : 0; return FG_OK;
+    case FG_OPT_CTAS_PER_SM: *value = (int)W->ctas_per_sm; return FG_OK;
+    case FG_OPT_AUTOTUNE_TILES: *value = (int)W->tune_tiles; return FG_OK;
     default: return FG_E_INVALID;
     }
 }

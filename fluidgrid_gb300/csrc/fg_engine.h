@@ -12,6 +12,10 @@ struct fg_scene_desc;
 
 namespace fg {
 
+#define FG_LIST_CAP_DEFAULT 160u
+#define FG_LIST_CAP_MAX 2048u
+#define FG_LIST_CHECK_PERIOD 25u
+
 void set_error(const char *what, cudaError_t e);
 void set_error_msg(const char *what);
 void fill_scene(FgScene &S, const fg_scene_desc &d);
@@ -32,11 +36,14 @@ struct World {
     float2 *dp = nullptr;
     uint32_t *keys_u = nullptr, *keys = nullptr, *ids = nullptr, *start = nullptr, *end = nullptr;
     RadixScratch rs{nullptr, nullptr, nullptr};
-    NbrList nbr{nullptr, nullptr, nullptr, 0}; /* density -> forces neighbour lists */
+    NbrList nbr{nullptr, nullptr, nullptr, 0, nullptr, nullptr}; /* density -> forces neighbour lists */
+    uint32_t list_cap_alloc = 0; /* list slots per particle allocated */
     uint32_t *inv = nullptr;  /* particle -> sorted index (written by the ranges pass) */
     uint32_t *tord = nullptr; /* spatial target order (particle ids, scene-contiguous) */
     bool use_list = true, use_order = false;
-    bool use_cc = false;       /* cell-cooperative density/forces (warp per bucket run) */
+    bool use_cc = false;       /* kernel 2: warp per bucket run, candidates staged in shared memory */
+    uint32_t ctas_per_sm = 0;  /* CTAs per SM of the density/force grids (0 = 16) */
+    int set_list_cap(uint32_t cap);
     uint32_t *runs = nullptr;  /* occupied-bucket run heads */
     uint32_t *nruns = nullptr; /* device counter */
     uint32_t order_period = 16, order_bits = 8, order_scene_shift = 24, order_key_bits = 24;
@@ -66,26 +73,42 @@ struct World {
     bool use_graphs = true;
     /* one instantiated step graph per configuration signature */
     struct CachedGraph {
-        uint32_t sig;
+        uint64_t sig;
         cudaGraph_t graph;
         cudaGraphExec_t exec;
     };
     std::vector<CachedGraph> graphs;
-    uint32_t graph_signature() const;
+    uint64_t graph_signature() const;
     int graph_for_current(cudaGraphExec_t *out);
-    /* online autotuner: every tune_period steps, each candidate kernel runs one
-     * (real) step under CUDA events and the fastest is kept */
+    /* online autotuner: every tune_period steps, each candidate value of one
+     * tunable (kernel, block warps, digit width; the tunable rotates) runs
+     * one real step under CUDA events and the fastest is kept */
     uint32_t tune_period = 25;
-    uint32_t tune_count[3] = {0, 0, 0}; /* steps run with kernel 0/1/2 */
+    uint32_t tune_count[3] = {0, 0, 0}; /* steps run with kernel 0..2 */
     float tune_last_ms[3] = {0.f, 0.f, 0.f};
-    uint32_t tune_kernels = 0x3; /* candidate kernels bit mask */
+    uint32_t tune_kernels = 0x2; /* candidate kernels bit mask */
+    uint32_t tune_tiles = 0x3;   /* 1: CTAs per SM, 2: digit width */
+    uint32_t tune_round = 0;
+    unsigned long long *overflow_counter = nullptr; /* list overflows since the last reset */
+    uint32_t *max_count = nullptr; /* largest list count since the last capacity check */
+    bool list_autogrow = true;     /* grow the list capacity to the largest count seen */
+    int check_list_cap();
     int current_kernel() const { return use_cc ? 2 : (use_list ? 1 : 0); }
     void set_kernel(int k)
     {
         use_cc = (k == 2);
         use_list = (k == 1);
     }
-    int tune_steps(uint32_t *done);
+    bool needs_runs() const { return use_cc; }
+    struct TuneRound {
+        bool active = false;
+        int dim = 0, ncand = 0, idx = 0;
+        int cand[4] = {0, 0, 0, 0};
+        cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    } tr;
+    void tune_begin();
+    void tune_apply(int dim, int v);
+    int tune_finish();
     std::vector<void *> allocs;
     size_t device_bytes = 0;
 

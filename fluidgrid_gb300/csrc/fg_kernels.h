@@ -18,6 +18,7 @@ struct Launch {
     uint32_t nwork;        /* work items */
     uint32_t n;            /* particles (single-scene mode) */
     cudaStream_t stream;
+    uint32_t ctas_per_sm;  /* density/force grids: CTAs per SM (0 = 16) */
 };
 
 int sm_count();
@@ -65,17 +66,21 @@ struct TargetOrder {
 /* ---- SPH (fg_sph.cu) ---- */
 
 /* In-range neighbour lists recorded by the density pass and consumed by the
- * force pass.  Slot k of sorted particle i is idx[k * stride + i] (SoA, so a
- * warp's stores and loads of one slot coalesce); cnt[i] is the number of
- * in-range bucket visits (may exceed FG_NBR_MAX, then forces re-walk the
- * buckets).  rec[2i] = (x, y, z, rho_i), rec[2i+1] = (vx, vy, vz, P_i): one
- * 32-byte sector per neighbour gather. */
-#define FG_NBR_MAX 96u
+ * force pass: the force pass's neighbours (l <= h, self excluded, duplicate
+ * bucket visits kept) in the bucket walk's order.  Target slot t owns
+ * idx[t * cap, (t + 1) * cap), cap a multiple of 4, written and read four
+ * entries (16 bytes) at a time, so each 32-byte sector is completed by two
+ * back-to-back stores of one thread instead of eight scattered 4-byte ones.
+ * cnt[t] may exceed cap; then the force pass re-walks the buckets.
+ * rec[2i] = (x, y, z, rho_i), rec[2i+1] = (vx, vy, vz, P_i): one 32-byte
+ * sector per neighbour gather. */
 struct NbrList {
     uint32_t *idx;
     uint32_t *cnt;
     float4 *rec;
-    uint32_t stride;
+    uint32_t cap;
+    uint32_t *max_count;          /* optional: atomicMax of cnt */
+    unsigned long long *overflow; /* optional: targets with cnt > cap */
 };
 
 void launch_density(const Launch &L, const float4 *spos, const uint32_t *start, const uint32_t *end, float2 *dp,

@@ -45,35 +45,8 @@ struct Kahan {
     }
 };
 
-/* Visit the particles of the 27 neighbour buckets in the reference's order
- * (z outer, x inner, each from -1 to 1; ascending sorted index inside a
- * bucket).  One runtime loop over the 27 buckets with the per-axis hashes
- * selected from registers: compact code (an unrolled walk multiplies the
- * body 27 times and thrashes the instruction cache) and no local memory. */
-template <typename Fn>
-__device__ __forceinline__ void fg_walk27(float px, float py, float pz, const FgScene *S,
-                                          const uint32_t *__restrict__ start, const uint32_t *__restrict__ end,
-                                          Fn &&fn)
-{
-    uint32_t hx[3], hy[3], hz[3];
-    fg_neighbour_hashes(px, py, pz, S->cell, hx, hy, hz);
-    const uint32_t hx0 = hx[0], hx1 = hx[1], hx2 = hx[2], hy0 = hy[0], hy1 = hy[1], hy2 = hy[2];
-    const uint32_t hz0 = hz[0], hz1 = hz[1], hz2 = hz[2];
-    const uint32_t nb = S->nb, mask = S->nb_mask, bb = S->bucket_base;
-#pragma unroll 1
-    for (int k = 0; k < 27; k++) {
-        const int z = k / 9, y = (k / 3) % 3, x = k % 3;
-        const uint32_t b = bb + fg_bucket(fg_sel3(hx0, hx1, hx2, x), fg_sel3(hy0, hy1, hy2, y),
-                                          fg_sel3(hz0, hz1, hz2, z), nb, mask);
-        const uint32_t st = __ldg(start + b);
-        if (st == FG_EMPTY) continue;
-        const uint32_t en = __ldg(end + b);
-        for (uint32_t j = st; j < en; j++) fn(j);
-    }
-}
-
 template <bool LIST>
-__global__ void __launch_bounds__(FG_CHUNK) k_density(const FgWork *__restrict__ work, uint32_t nwork,
+__global__ void __launch_bounds__(FG_CHUNK, 8) k_density(const FgWork *__restrict__ work, uint32_t nwork,
                                                      uint32_t n_single, const FgScene *__restrict__ table,
                                                      const __grid_constant__ FgScene single,
                                                      const float4 *__restrict__ spos,
@@ -85,6 +58,9 @@ __global__ void __launch_bounds__(FG_CHUNK) k_density(const FgWork *__restrict__
                                                      unsigned long long *__restrict__ pairs)
 {
     const uint32_t tid = threadIdx.x;
+    unsigned long long pc = 0; /* in-range density visits of this thread */
+    uint32_t mx = 0;           /* largest list count of this thread */
+    uint32_t ovf = 0;          /* targets of this thread with more entries than slots */
     for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
         FgWork it = fg_work(work, w, n_single);
         const bool valid = tid < it.count;
@@ -93,7 +69,10 @@ __global__ void __launch_bounds__(FG_CHUNK) k_density(const FgWork *__restrict__
         const uint32_t i = (ord.tord && valid) ? __ldg(ord.inv + __ldg(ord.tord + tpos)) : tpos;
         const float4 p = valid ? spos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const bool active = valid && p.w > 0.0f; /* inactive: density not written */
-        uint32_t cnt = 0;
+        uint32_t cnt = 0, dcnt = 0; /* list entries; density visits */
+        /* the last list entries not yet stored (stored four at a time) */
+        uint32_t q0 = 0, q1 = 0, q2 = 0, q3 = 0;
+        uint32_t *lp = LIST ? list.idx + (size_t)tpos * list.cap : nullptr;
         if (active) {
             const float scale = S->scale, h2 = S->h2;
             const float px = p.x * scale, py = p.y * scale, pz = p.z * scale;
@@ -102,16 +81,30 @@ __global__ void __launch_bounds__(FG_CHUNK) k_density(const FgWork *__restrict__
                 const float4 q = __ldg(spos + j);
                 const float dx = fmaf(-q.x, scale, px), dy = fmaf(-q.y, scale, py), dz = fmaf(-q.z, scale, pz);
                 const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                if (r2 < h2) {
+                if (r2 <= h2) {
+                    /* l < h adds (h^2 - l^2)^3; at l = h that is an exact 0 */
                     const float t = h2 - r2;
                     acc.add(t * t * t);
-                    /* straight to the SoA slot: the L2 merges the partial
-                     * sector writes, no shared-memory staging (which would
-                     * cost occupancy and L1 capacity) */
-                    if (LIST && cnt < FG_NBR_MAX) list.idx[(size_t)cnt * list.stride + tpos] = j;
-                    cnt++;
+                    dcnt++;
+                    /* the force pass's neighbours (l <= h, not itself) */
+                    if (LIST && j != i) {
+                        q0 = q1;
+                        q1 = q2;
+                        q2 = q3;
+                        q3 = j;
+                        cnt++;
+                        if ((cnt & 3u) == 0u && cnt <= list.cap)
+                            *reinterpret_cast<uint4 *>(lp + cnt - 4u) = make_uint4(q0, q1, q2, q3);
+                    }
                 }
             });
+            if (LIST && (cnt & 3u) && cnt < list.cap) {
+                /* the last 1..3 entries sit in q3, (q2, q3) or (q1, q2, q3) */
+                const uint32_t r = cnt & 3u;
+                const uint4 t = r == 1u ? make_uint4(q3, 0u, 0u, 0u)
+                                        : (r == 2u ? make_uint4(q2, q3, 0u, 0u) : make_uint4(q1, q2, q3, 0u));
+                *reinterpret_cast<uint4 *>(lp + (cnt & ~3u)) = t;
+            }
             const float mass = use_o ? mass_o : S->mass;
             const float gas = use_o ? gas_o : S->gas;
             const float rest = use_o ? rest_o : S->rest;
@@ -131,11 +124,24 @@ __global__ void __launch_bounds__(FG_CHUNK) k_density(const FgWork *__restrict__
             list.rec[2 * i + 1] = make_float4(v.x, v.y, v.z, d.y);
         }
         if (LIST && valid) list.cnt[tpos] = cnt;
-        if (pairs) {
-            /* in-range pair visits of this warp (self included), for reporting */
-            const uint32_t s = __reduce_add_sync(0xffffffffu, cnt);
-            if ((tid & 31) == 0 && s) atomicAdd(pairs, (unsigned long long)s);
-        }
+        pc += dcnt;
+        mx = max(mx, cnt);
+        ovf += (LIST && cnt > list.cap) ? 1u : 0u;
+    }
+    /* once per warp: in-range pair visits (self included) for reporting, and
+     * the largest list count for the capacity check */
+    if (pairs) {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) pc += __shfl_xor_sync(0xffffffffu, pc, o);
+        if ((tid & 31) == 0 && pc) atomicAdd(pairs, pc);
+    }
+    if (LIST && list.max_count) {
+        mx = __reduce_max_sync(0xffffffffu, mx);
+        if ((tid & 31) == 0 && mx) atomicMax(list.max_count, mx);
+    }
+    if (LIST && list.overflow) {
+        ovf = __reduce_add_sync(0xffffffffu, ovf);
+        if ((tid & 31) == 0 && ovf) atomicAdd(list.overflow, (unsigned long long)ovf);
     }
 }
 
@@ -144,7 +150,7 @@ void launch_density(const Launch &L, const float4 *spos, const uint32_t *start, 
                     TargetOrder ord, unsigned long long *pairs)
 {
     if (!L.nwork) return;
-    const uint32_t g = grid_for(L.nwork, 16);
+    const uint32_t g = grid_for(L.nwork, L.ctas_per_sm ? (int)L.ctas_per_sm : 16);
     if (list) {
         k_density<true><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, start,
                                                       end, dp, gas_o, rest_o, mass_o, use_o, *list, ord, pairs);
@@ -196,17 +202,31 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                 const float4 r0 = list.rec[2 * i], r1 = list.rec[2 * i + 1];
                 const float rho_i = r0.w, P_i = r1.w;
                 const uint32_t c = list.cnt[tpos];
-                if (c <= FG_NBR_MAX) {
-                    const uint32_t *nl = list.idx + tpos;
-#pragma unroll 2
-                    for (uint32_t k = 0; k < c; k++) {
-                        const uint32_t j = __ldg(nl + (size_t)k * list.stride);
-                        if (j == i) continue;
-                        const float4 q0 = __ldg(list.rec + 2 * j), q1 = __ldg(list.rec + 2 * j + 1);
-                        const float dx = fmaf(-q0.x, scale, px), dy = fmaf(-q0.y, scale, py),
-                                    dz = fmaf(-q0.z, scale, pz);
-                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                        fg_pair(fx, fy, fz, dx, dy, dz, r2, h, kspiky, kv, rho_i, P_i, v, q0.w, q1.w, q1);
+                if (c <= list.cap) {
+                    /* in-range neighbours without self, four indices per
+                     * 16-byte load, then all eight record loads in flight */
+                    const uint32_t *nl = list.idx + (size_t)tpos * list.cap;
+                    for (uint32_t k = 0; k < c; k += 4) {
+                        const uint4 q = __ldg(reinterpret_cast<const uint4 *>(nl + k));
+                        const uint32_t jj[4] = {q.x, q.y, q.z, q.w};
+                        const uint32_t m = min(4u, c - k);
+                        float4 a[4], b[4];
+#pragma unroll
+                        for (int e = 0; e < 4; e++) {
+                            const uint32_t j = (uint32_t)e < m ? jj[e] : jj[0];
+                            a[e] = __ldg(list.rec + 2 * j);
+                            b[e] = __ldg(list.rec + 2 * j + 1);
+                        }
+#pragma unroll
+                        for (int e = 0; e < 4; e++) {
+                            if ((uint32_t)e < m) {
+                                const float dx = fmaf(-a[e].x, scale, px), dy = fmaf(-a[e].y, scale, py),
+                                            dz = fmaf(-a[e].z, scale, pz);
+                                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                                fg_pair(fx, fy, fz, dx, dy, dz, r2, h, kspiky, kv, rho_i, P_i, v, a[e].w, b[e].w,
+                                        b[e]);
+                            }
+                        }
                     }
                 } else {
                     /* more in-range visits than list slots: walk the buckets */
@@ -285,7 +305,7 @@ void launch_forces(const Launch &L, const float4 *spos, const float4 *svel, cons
     memset(&R, 0, sizeof(R));
     if (rigid) { R.dyn = *rigid; R.use_dyn = 1; }
     if (statics) { R.sta = *statics; R.use_sta = 1; }
-    const uint32_t g = grid_for(L.nwork, 16);
+    const uint32_t g = grid_for(L.nwork, L.ctas_per_sm ? (int)L.ctas_per_sm : 16);
     if (list) {
         k_forces<true><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, dp, start,
                                                      end, ids, out.vel, out.pos, R, mass_o, visc_o, use_o, *list, ord);

@@ -42,79 +42,6 @@ struct CcArgs {
     uint32_t nscenes;
 };
 
-/* scene owning a global bucket key (scenes are ordered by bucket_base) */
-__device__ __forceinline__ uint32_t cc_scene_of(const FgScene *table, uint32_t nscenes, uint32_t key)
-{
-    if (!table) return 0;
-    uint32_t lo = 0, hi = nscenes;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(&table[mid].bucket_base) <= key) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
-/* The 9 per-axis neighbour cell indices that determine a particle's 27
- * buckets (fg_neighbour_hashes before the prime products). */
-struct Sig {
-    int v[9];
-};
-
-__device__ __forceinline__ Sig cc_sig(float px, float py, float pz, const float *cell)
-{
-    Sig s;
-#pragma unroll
-    for (int o = -1; o <= 1; o++) {
-        s.v[o + 1] = fg_axis_index_off(px, cell[0], o);
-        s.v[o + 4] = fg_axis_index_off(py, cell[1], o);
-        s.v[o + 7] = fg_axis_index_off(pz, cell[2], o);
-    }
-    return s;
-}
-
-/* Lanes 0..26 return bucket k = lane's (z, y, x) = (lane/9, lane/3 % 3,
- * lane % 3) start and count; lanes 27..31 return count 0. */
-__device__ __forceinline__ void cc_bucket_of_lane(const Sig &s, const FgScene *S, const uint32_t *__restrict__ start,
-                                                  const uint32_t *__restrict__ end, int lane, uint32_t &st,
-                                                  uint32_t &cnt)
-{
-    st = 0;
-    cnt = 0;
-    if (lane < 27) {
-        const int z = lane / 9, y = (lane / 3) % 3, x = lane % 3;
-        const uint32_t hx = fg_sel3((uint32_t)s.v[0], (uint32_t)s.v[1], (uint32_t)s.v[2], x) * FG_PX;
-        const uint32_t hy = fg_sel3((uint32_t)s.v[3], (uint32_t)s.v[4], (uint32_t)s.v[5], y) * FG_PY;
-        const uint32_t hz = fg_sel3((uint32_t)s.v[6], (uint32_t)s.v[7], (uint32_t)s.v[8], z) * FG_PZ;
-        const uint32_t b = S->bucket_base + fg_bucket(hx, hy, hz, S->nb, S->nb_mask);
-        const uint32_t a = __ldg(start + b);
-        const uint32_t z1 = __ldg(end + b); /* independent of `a`: one memory latency, not two */
-        if (a != FG_EMPTY) {
-            st = a;
-            cnt = z1 - a;
-        }
-    }
-}
-
-__device__ __forceinline__ uint32_t cc_excl_scan(uint32_t v, int lane, uint32_t &total)
-{
-    uint32_t x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    total = __shfl_sync(0xffffffffu, x, 31);
-    return x - v;
-}
-
-__device__ __forceinline__ float cc_sum(float v)
-{
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
 /* Stage candidates [c0, c0 + mc) of the 27-bucket sequence into shared
  * memory.  st/off are lane-resident (lane k holds bucket k); they are
  * published to the warp's shared table tab (27 offsets, 27 starts) so every

@@ -1,4 +1,4 @@
-/* Pair terms and rigid contact shared by the SPH force kernels. */
+/* Neighbour walks, pair terms and rigid contact shared by the SPH kernels. */
 #ifndef FG_SPH_COMMON_CUH
 #define FG_SPH_COMMON_CUH
 
@@ -6,6 +6,115 @@
 #include "fg_kernels.h"
 
 namespace fg {
+
+/* Visit the particles of the 27 neighbour buckets in the reference's order
+ * (z outer, x inner, each from -1 to 1; ascending sorted index inside a
+ * bucket).  The buckets are taken a row (three x offsets) at a time: the
+ * row's three start and three end words are loaded together, so a row costs
+ * one memory latency instead of six dependent ones.  One runtime loop with
+ * the per-axis hashes selected from registers keeps the code compact (an
+ * unrolled walk multiplies the body 27 times and thrashes the instruction
+ * cache) and uses no local memory. */
+template <typename Fn>
+__device__ __forceinline__ void fg_walk27(float px, float py, float pz, const FgScene *S,
+                                          const uint32_t *__restrict__ start, const uint32_t *__restrict__ end,
+                                          Fn &&fn)
+{
+    uint32_t hx[3], hy[3], hz[3];
+    fg_neighbour_hashes(px, py, pz, S->cell, hx, hy, hz);
+    const uint32_t hx0 = hx[0], hx1 = hx[1], hx2 = hx[2], hy0 = hy[0], hy1 = hy[1], hy2 = hy[2];
+    const uint32_t hz0 = hz[0], hz1 = hz[1], hz2 = hz[2];
+    const uint32_t nb = S->nb, mask = S->nb_mask, bb = S->bucket_base;
+#pragma unroll 1
+    for (int r = 0; r < 9; r++) {
+        const uint32_t yh = fg_sel3(hy0, hy1, hy2, r % 3), zh = fg_sel3(hz0, hz1, hz2, r / 3);
+        const uint32_t b0 = bb + fg_bucket(hx0, yh, zh, nb, mask);
+        const uint32_t b1 = bb + fg_bucket(hx1, yh, zh, nb, mask);
+        const uint32_t b2 = bb + fg_bucket(hx2, yh, zh, nb, mask);
+        const uint32_t s0 = __ldg(start + b0), s1 = __ldg(start + b1), s2 = __ldg(start + b2);
+        const uint32_t e0 = __ldg(end + b0), e1 = __ldg(end + b1), e2 = __ldg(end + b2);
+#pragma unroll 1
+        for (int x = 0; x < 3; x++) {
+            const uint32_t st = fg_sel3(s0, s1, s2, x);
+            if (st == FG_EMPTY) continue; /* end of an empty bucket is stale */
+            const uint32_t en = fg_sel3(e0, e1, e2, x);
+            for (uint32_t j = st; j < en; j++) fn(j);
+        }
+    }
+}
+
+/* scene owning a global bucket key (scenes are ordered by bucket_base) */
+__device__ __forceinline__ uint32_t cc_scene_of(const FgScene *table, uint32_t nscenes, uint32_t key)
+{
+    if (!table) return 0;
+    uint32_t lo = 0, hi = nscenes;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&table[mid].bucket_base) <= key) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+/* The 9 per-axis neighbour cell indices that determine a particle's 27
+ * buckets (fg_neighbour_hashes before the prime products). */
+struct Sig {
+    int v[9];
+};
+
+__device__ __forceinline__ Sig cc_sig(float px, float py, float pz, const float *cell)
+{
+    Sig s;
+#pragma unroll
+    for (int o = -1; o <= 1; o++) {
+        s.v[o + 1] = fg_axis_index_off(px, cell[0], o);
+        s.v[o + 4] = fg_axis_index_off(py, cell[1], o);
+        s.v[o + 7] = fg_axis_index_off(pz, cell[2], o);
+    }
+    return s;
+}
+
+/* Lanes 0..26 return bucket k = lane's (z, y, x) = (lane/9, lane/3 % 3,
+ * lane % 3) start and count; lanes 27..31 return count 0. */
+__device__ __forceinline__ void cc_bucket_of_lane(const Sig &s, const FgScene *S, const uint32_t *__restrict__ start,
+                                                  const uint32_t *__restrict__ end, int lane, uint32_t &st,
+                                                  uint32_t &cnt)
+{
+    st = 0;
+    cnt = 0;
+    if (lane < 27) {
+        const int z = lane / 9, y = (lane / 3) % 3, x = lane % 3;
+        const uint32_t hx = fg_sel3((uint32_t)s.v[0], (uint32_t)s.v[1], (uint32_t)s.v[2], x) * FG_PX;
+        const uint32_t hy = fg_sel3((uint32_t)s.v[3], (uint32_t)s.v[4], (uint32_t)s.v[5], y) * FG_PY;
+        const uint32_t hz = fg_sel3((uint32_t)s.v[6], (uint32_t)s.v[7], (uint32_t)s.v[8], z) * FG_PZ;
+        const uint32_t b = S->bucket_base + fg_bucket(hx, hy, hz, S->nb, S->nb_mask);
+        const uint32_t a = __ldg(start + b);
+        const uint32_t z1 = __ldg(end + b); /* independent of `a`: one memory latency, not two */
+        if (a != FG_EMPTY) {
+            st = a;
+            cnt = z1 - a;
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t cc_excl_scan(uint32_t v, int lane, uint32_t &total)
+{
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    total = __shfl_sync(0xffffffffu, x, 31);
+    return x - v;
+}
+
+__device__ __forceinline__ float cc_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
 
 /* Rigid-sphere contact of one fluid particle against a rigid grid
  * (ProcessCollisionForcesD with the per-body velocity of w, eps from the
@@ -58,7 +167,7 @@ __device__ __forceinline__ void fg_pair(float &fx, float &fy, float &fz, float d
     const float il = rsqrtf(r2);
     const float l = r2 * il;
     const float hl = h - l;
-    const float irr = __frcp_rn(rho_i * rho_j);
+    const float irr = __fdividef(1.0f, rho_i * rho_j); /* rho >= 1: no denormal or overflow range */
     /* pressure: -(d/l) kSpiky (h-l)^2 (Pi+Pj)/(rho_i rho_j) */
     const float cp = -(kspiky * hl * hl) * ((P_i + P_j) * irr) * il;
     /* viscosity: (vj-vi)/(rho_i rho_j) kVisc (h-l) mu */

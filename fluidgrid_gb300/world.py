@@ -128,12 +128,22 @@ class World:
               "fg_world_counters")
         return int(pv.value), int(st.value)
 
+    def list_overflows(self, reset=False):
+        """Particles (summed over steps) whose in-range visits exceeded the
+        neighbour-list capacity since the last reset."""
+        v = ctypes.c_uint64()
+        check(self.L.fg_world_list_overflows(self.h, 1 if reset else 0, ctypes.byref(v)), "fg_world_list_overflows")
+        return int(v.value)
+
     def tuning_stats(self):
-        """Steps run with each density/force kernel and the last trial times."""
-        cnt = (ctypes.c_uint32 * 3)()
-        ms = (ctypes.c_float * 3)()
+        """Steps run with each density/force kernel, the last kernel trial
+        times and the tunables in use."""
+        cnt = (ctypes.c_uint32 * _ffi.NUM_KERNELS)()
+        ms = (ctypes.c_float * _ffi.NUM_KERNELS)()
         check(self.L.fg_world_tuning_stats(self.h, cnt, ms), "fg_world_tuning_stats")
-        return {"steps_per_kernel": list(cnt), "last_trial_ms": [round(x, 4) for x in ms]}
+        return {"steps_per_kernel": list(cnt), "last_trial_ms": [round(x, 4) for x in ms],
+                "kernel": self.get_option("kernel"), "ctas_per_sm": self.get_option("ctas_per_sm"),
+                "digit_bits": self.get_option("digit_bits"), "list_cap": self.get_option("list_cap")}
 
     def launches_per_step(self):
         return int(self.L.fg_world_launches_per_step(self.h))

@@ -152,38 +152,61 @@ int fg_world_set_fused_integrate(fg_world *w, int fused);
 int fg_world_set_sort_digit_bits(fg_world *w, uint32_t bits);
 /* 1 = capture steps in a CUDA graph (default), 0 = direct launches */
 int fg_world_set_graphs(fg_world *w, int on);
-/* Tunables (picked by the autotuner; they change how work is scheduled, not
- * which neighbours are summed):
- *   FG_OPT_KERNEL         density/force kernels: 1 = one thread per particle
- *                         with in-range neighbour lists recorded by the
- *                         density pass (default), 0 = one thread per particle
- *                         walking the 27 buckets in both passes, 2 = one warp
- *                         per occupied bucket run with the 27 neighbour
- *                         buckets staged in shared memory
+/* Tunables (they change how work is scheduled, not which neighbours are
+ * summed):
+ *   FG_OPT_KERNEL         density/force kernels:
+ *                         1 = one thread per particle with in-range
+ *                             neighbour lists recorded by the density pass
+ *                             (default);
+ *                         0 = one thread per particle walking the 27 buckets
+ *                             in both passes;
+ *                         2 = one warp per run, one target at a time
  *   FG_OPT_NEIGHBOR_LIST  1 = kernel 1, 0 = kernel 0
  *   FG_OPT_TARGET_ORDER   kernels 0/1: 1 = targets in Morton order of their
  *                         cells, 0 = hashed bucket order (default)
  *   FG_OPT_ORDER_PERIOD   steps between refreshes of the Morton order (16)
  *   FG_OPT_DIGIT_BITS     radix digit width 1..8
- *   FG_OPT_AUTOTUNE_PERIOD  every this many steps, each candidate kernel
- *                         runs one (real) step under CUDA events and the
- *                         fastest is kept (0 = off; default 25): the best
- *                         kernel changes as a scene compresses
- *   FG_OPT_AUTOTUNE_KERNELS bit mask of candidate kernels (default 0x3)
+ *   FG_OPT_AUTOTUNE_PERIOD  every this many steps the autotuner runs one
+ *                         (real) step per candidate value of one tunable
+ *                         under CUDA events and keeps the fastest (0 = off;
+ *                         default 25): the best choice changes as a scene
+ *                         compresses
+ *   FG_OPT_AUTOTUNE_KERNELS bit mask of candidate kernels (default 0x2:
+ *                         kernel 1 only, so results never depend on timing)
+ *   FG_OPT_LIST_CAP       kernel 1: neighbour-list slots per particle, a
+ *                         multiple of 4 (default 160, at most 2048; values
+ *                         round up to a multiple of 4; a particle with more
+ *                         in-range visits re-walks its buckets in the force
+ *                         pass; a larger value reallocates the lists; setting
+ *                         it turns FG_OPT_LIST_AUTOGROW off)
+ *   FG_OPT_LIST_AUTOGROW  kernel 1: 1 = every 25 steps grow the capacity to
+ *                         1.125x the largest in-range count seen (default)
+ *   FG_OPT_CTAS_PER_SM    kernels 0/1: CTAs per SM of the persistent
+ *                         128-thread density/force grids (0 = 16)
+ *   FG_OPT_AUTOTUNE_TILES bit mask of the tunables the autotuner varies:
+ *                         1 = CTAs per SM, 2 = radix digit width (default 3)
  * Kernels 0 and 1 (with either target order) produce bit-identical states;
- * kernel 2 sums the same terms in a different order. */
+ * kernel 2 sums the same terms in another order.  No kernel's results depend
+ * on CTAs per SM or digit width, and kernel 1's not on the list capacity
+ * either (the list holds the bucket walk's order). */
 enum {
     FG_OPT_NEIGHBOR_LIST = 1, FG_OPT_TARGET_ORDER = 2, FG_OPT_ORDER_PERIOD = 3, FG_OPT_DIGIT_BITS = 4,
-    FG_OPT_KERNEL = 5, FG_OPT_AUTOTUNE_PERIOD = 6, FG_OPT_AUTOTUNE_KERNELS = 7
+    FG_OPT_KERNEL = 5, FG_OPT_AUTOTUNE_PERIOD = 6, FG_OPT_AUTOTUNE_KERNELS = 7, FG_OPT_LIST_CAP = 8,
+    FG_OPT_CTAS_PER_SM = 10, FG_OPT_AUTOTUNE_TILES = 11, FG_OPT_LIST_AUTOGROW = 12
 };
+#define FG_NUM_KERNELS 3
 int fg_world_set_option(fg_world *w, int option, int value);
 int fg_world_get_option(const fg_world *w, int option, int *value);
 /* In-range pair visits (self and duplicate-bucket visits included) counted by
- * the density passes of kernels 0/1 and the steps run since the last reset
- * (synchronises the world's stream). */
+ * the density pass and the steps run since the last reset (synchronises the
+ * world's stream). */
 int fg_world_counters(fg_world *w, int reset, uint64_t *pair_visits, uint64_t *steps);
+/* kernel 1: particles whose in-range visits exceeded the list capacity, summed
+ * over the steps since the last reset (synchronises the world's stream) */
+int fg_world_list_overflows(fg_world *w, int reset, uint64_t *particles);
 /* steps run with each kernel so far and the last autotuning trial times */
-int fg_world_tuning_stats(const fg_world *w, uint32_t steps_per_kernel[3], float last_trial_ms[3]);
+int fg_world_tuning_stats(const fg_world *w, uint32_t steps_per_kernel[FG_NUM_KERNELS],
+                          float last_trial_ms[FG_NUM_KERNELS]);
 
 /* number of kernel launches one step enqueues */
 uint32_t fg_world_launches_per_step(const fg_world *w);

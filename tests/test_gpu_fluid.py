@@ -181,6 +181,118 @@ def test_tunables_do_not_change_results(name):
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), k
 
 
+@pytest.mark.parametrize("name", ["dam_break_16k", "odd_buckets"])
+def test_launch_shape_does_not_change_results(name):
+    """CTAs per SM of the density/force grids and the radix digit width change
+    no bit of the evolved state."""
+    spec = VARIANTS[name]
+    outs = {}
+    for ctas, bits in ((0, 7), (8, 8), (64, 6), (1, 5), (3, 8), (17, 3)):
+        w = World([spec])
+        w.set_option("autotune_period", 0)
+        w.set_option("ctas_per_sm", ctas)
+        w.set_option("digit_bits", bits)
+        w.step(4)
+        p, v = w.download()
+        outs[(ctas, bits)] = (p, v, w.read("DP"))
+        w.close()
+    base = outs[(0, 7)]
+    for k, o in outs.items():
+        for a, b in zip(o, base):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), k
+
+
+def test_autotuner_keeps_results_and_reports():
+    """The autotuner varies the CTAs per SM and the digit width along the
+    trajectory; the results do not depend on them, so a tuned run equals an
+    untuned one bit for bit."""
+    spec = VARIANTS["dam_break_16k"]
+    res = []
+    for period in (0, 2):
+        w = World([spec])
+        w.set_option("autotune_period", period)
+        w.step(12)
+        p, v = w.download()
+        st = w.tuning_stats()
+        w_ctas = w.get_option("ctas_per_sm")
+        res.append((p, v))
+        w.close()
+    assert st["steps_per_kernel"][1] == 12
+    assert w_ctas in (8, 16, 64) and 6 <= st["digit_bits"] <= 8
+    for a, b in zip(res[0], res[1]):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_list_overflow_falls_back_to_bucket_walk():
+    """A neighbour-list capacity below the in-range count sends those
+    particles through the bucket walk in the force pass; results stay within
+    the oracle tolerances and the overflow counter sees them."""
+    spec = VARIANTS["dam_break_16k"]
+    rng = np.random.default_rng(13)
+    v0 = np.zeros((spec.n, 4), np.float32)
+    v0[:, :3] = rng.normal(0, 0.5, (spec.n, 3))
+    w = World([spec])
+    w.set_option("kernel", 1)
+    w.set_option("list_cap", 12)
+    assert w.get_option("list_cap") == 12
+    w.list_overflows(reset=True)
+    w.upload(spec.pos.copy(), v0)
+    w.step(1)
+    g = {k: w.read(k) for k in ("DP", "VEL", "POS")}
+    assert w.list_overflows() > spec.n // 2
+    w.close()
+    _forces_check(spec, spec.pos, v0, g)
+
+
+@pytest.mark.parametrize("cap", [1, 12, 40])
+def test_list_capacity_never_changes_kernel1_results(cap):
+    """Kernel 1's lists hold the bucket walk's order, so a particle that
+    overflows its list (and walks the buckets in the force pass) gets the
+    same bits as one that does not."""
+    spec = VARIANTS["dam_break_16k"]
+    outs = []
+    for c in (None, cap):
+        w = World([spec])
+        w.set_option("kernel", 1)
+        if c:
+            w.set_option("list_cap", c)
+        w.step(3)
+        outs.append(w.download())
+        w.close()
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_list_capacity_grows():
+    spec = VARIANTS["dam_break_16k"]
+    w = World([spec])
+    w.step(1)
+    w.set_option("list_cap", 301)  # reallocates the lists, drops captured graphs
+    assert w.get_option("list_cap") == 304  # rounded up to a multiple of 4
+    w.step(2)
+    w.check_finite()
+    assert w.list_overflows() == 0
+    w.close()
+
+
+def test_list_capacity_autogrows():
+    """With autogrow on, the capacity check every 25 steps raises a too-small
+    capacity above the largest in-range count, after which no particle takes
+    the bucket-walk fallback."""
+    spec = VARIANTS["dam_break_16k"]
+    w = World([spec])
+    w.set_option("list_cap", 8)
+    assert w.get_option("list_autogrow") == 0
+    w.set_option("list_autogrow", 1)
+    w.step(26)
+    assert w.get_option("list_cap") > 8
+    w.list_overflows(reset=True)
+    w.step(3)
+    assert w.list_overflows() == 0
+    w.check_finite()
+    w.close()
+
+
 @pytest.mark.parametrize("kernel", [0, 1, 2])
 def test_each_kernel_matches_oracle(kernel):
     """Every density/force kernel variant against the oracle from an
