@@ -64,6 +64,31 @@ class fg_scene_desc(ctypes.Structure):
                 ("rb_volume_max", c_f * 3)]
 
 
+class fg_server_config(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_particles", c_u32), ("max_admit_per_step", c_u32),
+                ("use_graphs", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+
+
+class fg_server_step_info(ctypes.Structure):
+    _fields_ = [("active_scenes", c_u32), ("admitted", c_u32), ("finished", c_u32), ("queued", c_u32),
+                ("active_particles", ctypes.c_uint64), ("step_ms", c_f), ("pad_", c_f),
+                ("wall_ms", ctypes.c_double), ("resident_bytes", ctypes.c_size_t)]
+
+
+class fg_request_info(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int), ("steps_done", c_u32), ("steps_total", c_u32), ("n_particles", c_u32),
+                ("submit_s", ctypes.c_double), ("admit_s", ctypes.c_double), ("done_s", ctypes.c_double),
+                ("resident_bytes", ctypes.c_size_t)]
+
+
+class fg_server_stats_info(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_uint64), ("particle_steps", ctypes.c_uint64), ("queued", c_u32),
+                ("active", c_u32), ("resident_bytes", ctypes.c_size_t), ("resident_particles", ctypes.c_uint64),
+                ("device_bytes", ctypes.c_size_t)]
+
+
+REQ_QUEUED, REQ_ACTIVE, REQ_DONE = 0, 1, 2
+
 # buffer ids (fg_buffer_id)
 BUFFERS = ["POS", "VEL", "KEYS_UNSORTED", "KEYS", "IDS", "START", "END", "SPOS", "SVEL", "DP",
            "RB_LOCAL", "RB_WORLD", "RB_KEYS_UNSORTED", "RB_KEYS", "RB_IDS", "RB_START", "RB_END", "RB_SPOS",
@@ -92,7 +117,9 @@ C_ABI_SYMBOLS = [
     "fg_world_set_graphs", "fg_world_launches_per_step", "fg_world_stage_profile", "fg_world_timed_steps",
     "fg_world_e2e_steps", "fg_host_alloc", "fg_host_free", "fg_set_device", "fg_probe_fp32_peak",
     "fg_sort_pairs_noalloc", "fg_world_set_option", "fg_world_get_option", "fg_world_tuning_stats",
-    "fg_world_counters", "fg_world_list_overflows",
+    "fg_world_counters", "fg_world_list_overflows", "fg_server_config_defaults", "fg_server_create",
+    "fg_server_destroy", "fg_server_submit", "fg_server_step", "fg_server_request", "fg_server_result",
+    "fg_server_stats",
     "fg_memcpy_d2h", "fg_memcpy_h2d",
     "fg_device_synchronize", "fg_last_error", "fg_version"]
 REFERENCE_SYMBOLS = [
@@ -157,6 +184,16 @@ def load():
     L.fg_world_tuning_stats.argtypes = [VP, P(c_u32), P(c_f)]
     L.fg_world_counters.argtypes = [VP, ctypes.c_int, P(ctypes.c_uint64), P(ctypes.c_uint64)]
     L.fg_world_list_overflows.argtypes = [VP, ctypes.c_int, P(ctypes.c_uint64)]
+    L.fg_server_config_defaults.argtypes = [P(fg_server_config)]
+    L.fg_server_config_defaults.restype = None
+    L.fg_server_create.argtypes = [P(fg_server_config), VP, P(VP)]
+    L.fg_server_destroy.argtypes = [VP]
+    L.fg_server_destroy.restype = None
+    L.fg_server_submit.argtypes = [VP, P(fg_scene_desc), c_u32, P(ctypes.c_uint64)]
+    L.fg_server_step.argtypes = [VP, P(fg_server_step_info)]
+    L.fg_server_request.argtypes = [VP, ctypes.c_uint64, P(fg_request_info)]
+    L.fg_server_result.argtypes = [VP, ctypes.c_uint64, VP, VP, ctypes.c_int]
+    L.fg_server_stats.argtypes = [VP, P(fg_server_stats_info)]
     L.fg_memcpy_d2h.argtypes = [VP, VP, ctypes.c_size_t]
     L.fg_memcpy_h2d.argtypes = [VP, VP, ctypes.c_size_t]
     L.fg_last_error.restype = ctypes.c_char_p

@@ -187,25 +187,167 @@ static void build_work(std::vector<FgWork> &wt, uint32_t scene, uint32_t first, 
     }
 }
 
-int World::create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st)
+/* Element counts a set of scenes needs. */
+Capacity World::needs(const fg_scene_desc *d, uint32_t ns)
 {
-    nscenes = ns;
-    (void)sm_count(); /* cache the device query outside any graph capture */
-    if (st) {
-        stream = st;
-        own_stream = false;
-    } else {
-        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-        own_stream = true;
-    }
-    scenes_h.resize(ns);
-    uint64_t np = 0, nbk = 0, nsph = 0, nbod = 0, nrbk = 0;
+    Capacity c;
+    c.scenes = ns;
     for (uint32_t s = 0; s < ns; s++) {
-        int v = validate(d[s]);
-        if (v != FG_OK) {
-            set_error_msg("invalid scene description");
-            return v;
-        }
+        const uint64_t nb = (uint64_t)d[s].bucket_size[0] * d[s].bucket_size[1] * d[s].bucket_size[2];
+        uint64_t sph = 0;
+        for (uint32_t b = 0; b < d[s].n_bodies; b++) sph += d[s].bodies[b].n_spheres;
+        c.particles += d[s].n_particles;
+        c.buckets += nb;
+        c.spheres += sph;
+        c.bodies += d[s].n_bodies;
+        if (d[s].n_bodies)
+            c.rb_buckets += (uint64_t)d[s].rb_bucket_size[0] * d[s].rb_bucket_size[1] * d[s].rb_bucket_size[2];
+        c.work += (d[s].n_particles + FG_CHUNK - 1) / FG_CHUNK;
+        c.work_sph += (sph + FG_CHUNK - 1) / FG_CHUNK;
+    }
+    return c;
+}
+
+bool Capacity::fits(const Capacity &o) const
+{
+    return o.particles <= particles && o.buckets <= buckets && o.spheres <= spheres && o.bodies <= bodies &&
+           o.rb_buckets <= rb_buckets && o.scenes <= scenes && o.work <= work && o.work_sph <= work_sph;
+}
+
+bool Capacity::too_large() const
+{
+    return particles >= 0x7fffffffULL || buckets >= 0x7fffffffULL || spheres >= 0x7fffffffULL ||
+           rb_buckets >= 0x7fffffffULL;
+}
+
+/* Device bytes reserve(c) allocates (list capacity `list_cap` slots). */
+size_t World::footprint(const Capacity &c, uint32_t list_cap)
+{
+    const size_t P = std::max<uint64_t>(c.particles, 1), S = std::max<uint64_t>(c.spheres, 1);
+    const size_t M = std::max(P, S);
+    size_t b = 0;
+    b += P * (16 + 16 + 4 + 4 + 4 + 16 + 16 + 8); /* pos vel keys_u keys ids spos svel dp */
+    b += M * 8 + 4 * radix_hist_words((uint32_t)M); /* sort scratch */
+    b += P * (4 * (size_t)list_cap + 4 + 32);      /* lists, counts, records */
+    b += P * 12;                                    /* runs, inv, tord */
+    b += 8 * std::max<uint64_t>(c.buckets, 1);
+    b += (sizeof(FgScene) + 24) * std::max<uint64_t>(c.scenes, 1);
+    b += sizeof(FgWork) * (std::max<uint64_t>(c.work, 1) + std::max<uint64_t>(c.work_sph, 1));
+    if (c.bodies) {
+        b += S * (16 * 6 + 12);
+        b += 8 * std::max<uint64_t>(c.rb_buckets, 1);
+        b += c.bodies * (32 * 6 + 16 * 3 + 8 + 72 + 12);
+    }
+    return b;
+}
+
+/* Allocate every buffer for capacity c (once per World). */
+int World::reserve(const Capacity &c)
+{
+    cap = c;
+    int r;
+    auto A = [&](void **p, size_t b) { return alloc(p, b); };
+    const size_t Sc = std::max<uint64_t>(c.scenes, 1);
+    if ((r = A((void **)&scenes_d, sizeof(FgScene) * Sc))) return r;
+    if ((r = A((void **)&work_d, sizeof(FgWork) * std::max<uint64_t>(c.work, 1)))) return r;
+    if ((r = A((void **)&work_sph_d, sizeof(FgWork) * std::max<uint64_t>(c.work_sph, 1)))) return r;
+    const size_t N = std::max<uint64_t>(c.particles, 1);
+    const size_t NB = std::max<uint64_t>(c.buckets, 1);
+    if ((r = A((void **)&pos, 16 * N))) return r;
+    if ((r = A((void **)&vel, 16 * N))) return r;
+    if ((r = A((void **)&keys_u, 4 * N))) return r;
+    if ((r = A((void **)&keys, 4 * N))) return r;
+    if ((r = A((void **)&ids, 4 * N))) return r;
+    if ((r = A((void **)&spos, 16 * N))) return r;
+    if ((r = A((void **)&svel, 16 * N))) return r;
+    if ((r = A((void **)&dp, 8 * N))) return r;
+    if ((r = A((void **)&start, 4 * NB))) return r;
+    if ((r = A((void **)&end, 4 * NB))) return r;
+    const size_t M = std::max(N, (size_t)std::max<uint64_t>(c.spheres, 1));
+    if ((r = A((void **)&rs.keys_alt, 4 * M))) return r;
+    if ((r = A((void **)&rs.vals_alt, 4 * M))) return r;
+    if ((r = A((void **)&rs.hist, 4 * radix_hist_words((uint32_t)M)))) return r;
+    if (!list_cap_alloc) list_cap_alloc = FG_LIST_CAP_DEFAULT;
+    if ((r = A((void **)&nbr.idx, 4 * (size_t)list_cap_alloc * N))) return r;
+    nbr.cap = list_cap_alloc;
+    if ((r = A((void **)&nbr.cnt, 4 * N))) return r;
+    if ((r = A((void **)&nbr.rec, 32 * N))) return r;
+    if ((r = A((void **)&runs, 4 * N))) return r;
+    if ((r = A((void **)&nruns, 16))) return r;
+    if ((r = A((void **)&inv, 4 * N))) return r;
+    if ((r = A((void **)&tord, 4 * N))) return r;
+    if ((r = A((void **)&status_d, 64))) return r;
+    CK(cudaMemsetAsync(status_d, 0, 64, stream));
+    pair_counter = (unsigned long long *)(status_d + 8); /* 8-byte aligned slots of the status block */
+    overflow_counter = (unsigned long long *)(status_d + 10);
+    max_count = status_d + 12;
+    nbr.max_count = max_count;
+    nbr.overflow = overflow_counter;
+    CK(cudaMemsetAsync(dp, 0, 8 * N, stream));
+    CK(cudaMemsetAsync(vel, 0, 16 * N, stream));
+    CK(cudaMemsetAsync(end, 0, 4 * NB, stream));
+    /* lists read before any density pass (stage-split calls) see zero
+     * counts and in-range indices */
+    CK(cudaMemsetAsync(nbr.cnt, 0, 4 * N, stream));
+    CK(cudaMemsetAsync(nbr.idx, 0, 4 * (size_t)list_cap_alloc * N, stream));
+    CK(cudaMemsetAsync(nbr.rec, 0, 32 * N, stream));
+    if ((r = A((void **)&aabb, 24 * Sc))) return r;
+    if (c.bodies) {
+        const size_t S = std::max<uint64_t>(c.spheres, 1), B = c.bodies;
+        const size_t RB = std::max<uint64_t>(c.rb_buckets, 1);
+        if ((r = A((void **)&rb_local, 16 * S))) return r;
+        if ((r = A((void **)&rb_world, 16 * S))) return r;
+        if ((r = A((void **)&rb_keys_u, 4 * S))) return r;
+        if ((r = A((void **)&rb_keys, 4 * S))) return r;
+        if ((r = A((void **)&rb_ids, 4 * S))) return r;
+        if ((r = A((void **)&rb_spos, 16 * S))) return r;
+        if ((r = A((void **)&rb_force, 16 * S))) return r;
+        if ((r = A((void **)&rb_torque, 16 * S))) return r;
+        if ((r = A((void **)&rb_start, 4 * RB))) return r;
+        if ((r = A((void **)&rb_end, 4 * RB))) return r;
+        if ((r = A((void **)&bx, 32 * B))) return r;
+        if ((r = A((void **)&bv, 32 * B))) return r;
+        if ((r = A((void **)&bq, 32 * B))) return r;
+        if ((r = A((void **)&bL, 32 * B))) return r;
+        if ((r = A((void **)&bfs, 32 * B))) return r;
+        if ((r = A((void **)&bts, 32 * B))) return r;
+        if ((r = A((void **)&bxf, 16 * B))) return r;
+        if ((r = A((void **)&bvf, 16 * B))) return r;
+        if ((r = A((void **)&bqf, 16 * B))) return r;
+        if ((r = A((void **)&bmass, 8 * B))) return r;
+        if ((r = A((void **)&binv, 72 * B))) return r;
+        if ((r = A((void **)&body_scene, 4 * B))) return r;
+        if ((r = A((void **)&body_first, 4 * B))) return r;
+        if ((r = A((void **)&body_count, 4 * B))) return r;
+        CK(cudaMemsetAsync(rb_end, 0, 4 * RB, stream));
+        CK(cudaMemsetAsync(bfs, 0, 32 * B, stream));
+        CK(cudaMemsetAsync(bts, 0, 32 * B, stream));
+    }
+    return FG_OK;
+}
+
+/* Scene table, work tables and the static per-body and per-sphere data of
+ * the scenes d[0..ns) (which must fit the capacity).  Dynamic state --
+ * particle positions, velocities, densities and the bodies' motion -- is not
+ * touched: upload_scene or a migration fills it. */
+int World::set_layout(const fg_scene_desc *d, uint32_t ns)
+{
+    const Capacity need = needs(d, ns);
+    if (need.too_large()) {
+        set_error_msg("world too large");
+        return FG_E_INVALID;
+    }
+    if (!cap.fits(need) || (need.bodies && !rb_local)) {
+        set_error_msg("scenes exceed the world's capacity");
+        return FG_E_BUDGET;
+    }
+    /* steps in flight read the tables rewritten below */
+    CK(cudaStreamSynchronize(stream));
+    nscenes = ns;
+    scenes_h.assign(std::max<uint32_t>(ns, 1), FgScene{});
+    uint64_t np = 0, nbk = 0, nsph = 0, nbod = 0, nrbk = 0;
+    any_rb_rb = false;
+    for (uint32_t s = 0; s < ns; s++) {
         FgScene &S = scenes_h[s];
         fill_scene(S, d[s]);
         S.pbase = (uint32_t)np;
@@ -221,22 +363,20 @@ int World::create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st)
         nsph += sph;
         nbod += d[s].n_bodies;
         if (d[s].n_bodies) nrbk += S.rb_nb;
-    }
-    if (np >= 0x7fffffffULL || nbk >= 0x7fffffffULL || nsph >= 0x7fffffffULL || nrbk >= 0x7fffffffULL) {
-        set_error_msg("world too large");
-        return FG_E_INVALID;
+        if (d[s].n_bodies && d[s].rb_rb_contact) any_rb_rb = true;
     }
     n = (uint32_t)np;
     total_buckets = (uint32_t)nbk;
     nspheres = (uint32_t)nsph;
     nbodies = (uint32_t)nbod;
     total_rb_buckets = (uint32_t)nrbk;
+    const uint32_t old_key_bits = key_bits;
     key_bits = ceil_log2(total_buckets);
     rb_key_bits = ceil_log2(std::max<uint32_t>(total_rb_buckets, 1));
-    digit_bits = key_bits <= 16 ? std::max<uint32_t>(1, (key_bits + 1) / 2) : (key_bits + 2) / 3;
-    if (digit_bits > 8) digit_bits = 8;
-
-    /* work tables */
+    if (!digit_bits || key_bits != old_key_bits) {
+        digit_bits = key_bits <= 16 ? std::max<uint32_t>(1, (key_bits + 1) / 2) : (key_bits + 2) / 3;
+        if (digit_bits > 8) digit_bits = 8;
+    }
     std::vector<FgWork> fw, sw;
     for (uint32_t s = 0; s < ns; s++) {
         build_work(fw, s, scenes_h[s].pbase, scenes_h[s].n);
@@ -245,91 +385,21 @@ int World::create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st)
     nwork = (uint32_t)fw.size();
     nwork_sph = (uint32_t)sw.size();
     single = (ns == 1);
-
-    int r;
-    auto A = [&](void **p, size_t b) { return alloc(p, b); };
-    if ((r = A((void **)&scenes_d, sizeof(FgScene) * std::max<uint32_t>(ns, 1)))) return r;
-    if ((r = A((void **)&work_d, sizeof(FgWork) * std::max<uint32_t>(nwork, 1)))) return r;
-    if ((r = A((void **)&work_sph_d, sizeof(FgWork) * std::max<uint32_t>(nwork_sph, 1)))) return r;
-    const size_t N = std::max<uint32_t>(n, 1);
-    if ((r = A((void **)&pos, 16 * N))) return r;
-    if ((r = A((void **)&vel, 16 * N))) return r;
-    if ((r = A((void **)&keys_u, 4 * N))) return r;
-    if ((r = A((void **)&keys, 4 * N))) return r;
-    if ((r = A((void **)&ids, 4 * N))) return r;
-    if ((r = A((void **)&spos, 16 * N))) return r;
-    if ((r = A((void **)&svel, 16 * N))) return r;
-    if ((r = A((void **)&dp, 8 * N))) return r;
-    if ((r = A((void **)&start, 4 * (size_t)std::max<uint32_t>(total_buckets, 1)))) return r;
-    if ((r = A((void **)&end, 4 * (size_t)std::max<uint32_t>(total_buckets, 1)))) return r;
-    const size_t M = std::max(N, (size_t)std::max<uint32_t>(nspheres, 1));
-    if ((r = A((void **)&rs.keys_alt, 4 * M))) return r;
-    if ((r = A((void **)&rs.vals_alt, 4 * M))) return r;
-    if ((r = A((void **)&rs.hist, 4 * radix_hist_words((uint32_t)M)))) return r;
-    list_cap_alloc = FG_LIST_CAP_DEFAULT;
-    if ((r = A((void **)&nbr.idx, 4 * (size_t)list_cap_alloc * N))) return r;
-    nbr.cap = list_cap_alloc;
-    nbr.max_count = nullptr;
-    if ((r = A((void **)&nbr.cnt, 4 * N))) return r;
-    if ((r = A((void **)&nbr.rec, 32 * N))) return r;
-    if ((r = A((void **)&runs, 4 * N))) return r;
-    if ((r = A((void **)&nruns, 16))) return r;
-    if ((r = A((void **)&inv, 4 * N))) return r;
-    if ((r = A((void **)&tord, 4 * N))) return r;
     {
-        const uint32_t sbits = ceil_log2(ns);
+        const uint32_t sbits = ceil_log2(std::max<uint32_t>(ns, 1));
         order_bits = std::min<uint32_t>(10u, (32u - sbits) / 3u);
         order_scene_shift = 3u * order_bits;
         order_key_bits = order_scene_shift + sbits;
     }
-    if ((r = A((void **)&status_d, 64))) return r;
-    CK(cudaMemsetAsync(status_d, 0, 64, stream));
-    pair_counter = (unsigned long long *)(status_d + 8); /* 8-byte aligned slots of the status block */
-    overflow_counter = (unsigned long long *)(status_d + 10);
-    max_count = status_d + 12;
-    nbr.max_count = max_count;
-    nbr.overflow = overflow_counter;
-    CK(cudaMemsetAsync(dp, 0, 8 * N, stream));
-    /* lists read before any density pass (stage-split calls) see zero
-     * counts and in-range indices */
-    CK(cudaMemsetAsync(nbr.cnt, 0, 4 * N, stream));
-    CK(cudaMemsetAsync(nbr.idx, 0, 4 * (size_t)list_cap_alloc * N, stream));
-    CK(cudaMemsetAsync(nbr.rec, 0, 32 * N, stream));
-    CK(cudaMemsetAsync(vel, 0, 16 * N, stream));
-    CK(cudaMemsetAsync(end, 0, 4 * (size_t)std::max<uint32_t>(total_buckets, 1), stream));
-
+    order_valid = false;
+    if (ns) CK(cudaMemcpyAsync(scenes_d, scenes_h.data(), sizeof(FgScene) * ns, cudaMemcpyHostToDevice, stream));
+    if (nwork) CK(cudaMemcpyAsync(work_d, fw.data(), sizeof(FgWork) * nwork, cudaMemcpyHostToDevice, stream));
+    if (nwork_sph)
+        CK(cudaMemcpyAsync(work_sph_d, sw.data(), sizeof(FgWork) * nwork_sph, cudaMemcpyHostToDevice, stream));
     if (nbodies) {
-        const size_t S = std::max<uint32_t>(nspheres, 1), B = nbodies;
-        if ((r = A((void **)&rb_local, 16 * S))) return r;
-        if ((r = A((void **)&rb_world, 16 * S))) return r;
-        if ((r = A((void **)&rb_keys_u, 4 * S))) return r;
-        if ((r = A((void **)&rb_keys, 4 * S))) return r;
-        if ((r = A((void **)&rb_ids, 4 * S))) return r;
-        if ((r = A((void **)&rb_spos, 16 * S))) return r;
-        if ((r = A((void **)&rb_force, 16 * S))) return r;
-        if ((r = A((void **)&rb_torque, 16 * S))) return r;
-        if ((r = A((void **)&rb_start, 4 * (size_t)std::max<uint32_t>(total_rb_buckets, 1)))) return r;
-        if ((r = A((void **)&rb_end, 4 * (size_t)std::max<uint32_t>(total_rb_buckets, 1)))) return r;
-        if ((r = A((void **)&aabb, 24 * (size_t)ns))) return r;
-        if ((r = A((void **)&bx, 32 * B))) return r;
-        if ((r = A((void **)&bv, 32 * B))) return r;
-        if ((r = A((void **)&bq, 32 * B))) return r;
-        if ((r = A((void **)&bL, 32 * B))) return r;
-        if ((r = A((void **)&bfs, 32 * B))) return r;
-        if ((r = A((void **)&bts, 32 * B))) return r;
-        if ((r = A((void **)&bxf, 16 * B))) return r;
-        if ((r = A((void **)&bvf, 16 * B))) return r;
-        if ((r = A((void **)&bqf, 16 * B))) return r;
-        if ((r = A((void **)&bmass, 8 * B))) return r;
-        if ((r = A((void **)&binv, 72 * B))) return r;
-        if ((r = A((void **)&body_scene, 4 * B))) return r;
-        if ((r = A((void **)&body_first, 4 * B))) return r;
-        if ((r = A((void **)&body_count, 4 * B))) return r;
-        CK(cudaMemsetAsync(rb_end, 0, 4 * (size_t)std::max<uint32_t>(total_rb_buckets, 1), stream));
-        /* host staging of bodies */
-        std::vector<float> local(4 * S, 0.0f);
-        std::vector<double> hx(4 * B), hv(4 * B, 0.0), hq(4 * B), hL(4 * B, 0.0), hm(B), hinv(9 * B);
-        std::vector<float> hxf(4 * B), hvf(4 * B, 0.0f), hqf(4 * B);
+        const size_t S = nspheres, B = nbodies;
+        std::vector<float> local(4 * std::max<size_t>(S, 1), 0.0f);
+        std::vector<double> hm(B), hinv(9 * B);
         std::vector<uint32_t> hbs(B), hbf(B), hbc(B);
         uint32_t gb = 0, gs = 0;
         for (uint32_t s = 0; s < ns; s++)
@@ -344,44 +414,101 @@ int World::create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st)
                     local[4 * gs + 2] = bd.local_spheres[4 * k + 2];
                     local[4 * gs + 3] = (float)gb; /* w = global body index */
                 }
-                for (int c = 0; c < 3; c++) hx[4 * gb + c] = bd.position[c];
-                hx[4 * gb + 3] = 0.0;
-                for (int c = 0; c < 4; c++) hq[4 * gb + c] = bd.orientation[c];
                 hm[gb] = bd.mass;
                 for (int c = 0; c < 9; c++) hinv[9 * gb + c] = bd.inv_inertia[c];
-                for (int c = 0; c < 4; c++) {
-                    hxf[4 * gb + c] = (float)hx[4 * gb + c];
-                    hqf[4 * gb + c] = (float)hq[4 * gb + c];
-                }
             }
-        CK(cudaMemcpy(rb_local, local.data(), 16 * (size_t)nspheres, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(bx, hx.data(), 32 * B, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(bv, hv.data(), 32 * B, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(bq, hq.data(), 32 * B, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(bL, hL.data(), 32 * B, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(bxf, hxf.data(), 16 * B, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(bvf, hvf.data(), 16 * B, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(bqf, hqf.data(), 16 * B, cudaMemcpyHostToDevice));
+        if (S) CK(cudaMemcpy(rb_local, local.data(), 16 * S, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(bmass, hm.data(), 8 * B, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(binv, hinv.data(), 72 * B, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(body_scene, hbs.data(), 4 * B, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(body_first, hbf.data(), 4 * B, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(body_count, hbc.data(), 4 * B, cudaMemcpyHostToDevice));
-        CK(cudaMemsetAsync(bfs, 0, 32 * B, stream));
-        CK(cudaMemsetAsync(bts, 0, 32 * B, stream));
     }
-    CK(cudaMemcpy(scenes_d, scenes_h.data(), sizeof(FgScene) * ns, cudaMemcpyHostToDevice));
-    if (nwork) CK(cudaMemcpy(work_d, fw.data(), sizeof(FgWork) * nwork, cudaMemcpyHostToDevice));
-    if (nwork_sph) CK(cudaMemcpy(work_sph_d, sw.data(), sizeof(FgWork) * nwork_sph, cudaMemcpyHostToDevice));
+    drop_graphs();
+    return FG_OK;
+}
 
-    /* initial state */
-    for (uint32_t s = 0; s < ns; s++) {
-        const FgScene &S = scenes_h[s];
-        if (!S.n) continue;
-        CK(cudaMemcpy(pos + S.pbase, d[s].positions, 16 * (size_t)S.n, cudaMemcpyHostToDevice));
-        if (d[s].velocities)
-            CK(cudaMemcpy(vel + S.pbase, d[s].velocities, 16 * (size_t)S.n, cudaMemcpyHostToDevice));
+/* Initial dynamic state of scene s from its description: positions,
+ * velocities (zero if none) and the bodies at rest at their poses. */
+int World::upload_scene(uint32_t s, const fg_scene_desc &d)
+{
+    const FgScene &S = scenes_h[s];
+    if (S.n) {
+        CK(cudaMemcpyAsync(pos + S.pbase, d.positions, 16 * (size_t)S.n, cudaMemcpyHostToDevice, stream));
+        if (d.velocities)
+            CK(cudaMemcpyAsync(vel + S.pbase, d.velocities, 16 * (size_t)S.n, cudaMemcpyHostToDevice, stream));
+        else
+            CK(cudaMemsetAsync(vel + S.pbase, 0, 16 * (size_t)S.n, stream));
+        CK(cudaMemsetAsync(dp + S.pbase, 0, 8 * (size_t)S.n, stream));
     }
+    if (S.nbodies) {
+        const size_t B = S.nbodies;
+        std::vector<double> hx(4 * B), hv(4 * B, 0.0), hq(4 * B), hL(4 * B, 0.0);
+        std::vector<float> hxf(4 * B), hvf(4 * B, 0.0f), hqf(4 * B);
+        for (uint32_t b = 0; b < S.nbodies; b++) {
+            const fg_body_desc &bd = d.bodies[b];
+            for (int c = 0; c < 3; c++) hx[4 * b + c] = bd.position[c];
+            hx[4 * b + 3] = 0.0;
+            for (int c = 0; c < 4; c++) hq[4 * b + c] = bd.orientation[c];
+            for (int c = 0; c < 4; c++) {
+                hxf[4 * b + c] = (float)hx[4 * b + c];
+                hqf[4 * b + c] = (float)hq[4 * b + c];
+            }
+        }
+        const size_t o = S.body_base;
+        CK(cudaMemcpy(bx + o, hx.data(), 32 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bv + o, hv.data(), 32 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bq + o, hq.data(), 32 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bL + o, hL.data(), 32 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bxf + o, hxf.data(), 16 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bvf + o, hvf.data(), 16 * B, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(bqf + o, hqf.data(), 16 * B, cudaMemcpyHostToDevice));
+    }
+    return FG_OK;
+}
+
+void World::drop_graphs()
+{
+    for (auto &g : graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        if (g.graph) cudaGraphDestroy(g.graph);
+    }
+    graphs.clear();
+}
+
+int World::init_stream(cudaStream_t st)
+{
+    (void)sm_count(); /* cache the device query outside any graph capture */
+    if (st) {
+        stream = st;
+        own_stream = false;
+    } else {
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        own_stream = true;
+    }
+    return FG_OK;
+}
+
+int World::create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st)
+{
+    int r = init_stream(st);
+    if (r != FG_OK) return r;
+    for (uint32_t s = 0; s < ns; s++) {
+        const int v = validate(d[s]);
+        if (v != FG_OK) {
+            set_error_msg("invalid scene description");
+            return v;
+        }
+    }
+    const Capacity c = needs(d, ns);
+    if (c.too_large()) {
+        set_error_msg("world too large");
+        return FG_E_INVALID;
+    }
+    if ((r = reserve(c)) != FG_OK) return r;
+    if ((r = set_layout(d, ns)) != FG_OK) return r;
+    for (uint32_t s = 0; s < ns; s++)
+        if ((r = upload_scene(s, d[s])) != FG_OK) return r;
     CK(cudaStreamSynchronize(stream));
     return FG_OK;
 }
@@ -547,30 +674,25 @@ uint64_t World::graph_signature() const
            ((uint64_t)nbr.cap << 32);
 }
 
-int World::set_list_cap(uint32_t cap)
+int World::set_list_cap(uint32_t slots)
 {
-    if (cap < 1 || cap > FG_LIST_CAP_MAX) return FG_E_INVALID;
-    cap = (cap + 3u) & ~3u; /* lists are stored four entries at a time */
-    if (cap > list_cap_alloc) {
+    if (slots < 1 || slots > FG_LIST_CAP_MAX) return FG_E_INVALID;
+    slots = (slots + 3u) & ~3u; /* lists are stored four entries at a time */
+    if (slots > list_cap_alloc) {
         CK(cudaStreamSynchronize(stream));
-        const size_t N = std::max<uint32_t>(n, 1);
+        const size_t N = std::max<uint64_t>(cap.particles, 1);
         uint32_t *p = nullptr;
-        CK(cudaMalloc(&p, 4 * (size_t)cap * N));
-        CK(cudaMemsetAsync(p, 0, 4 * (size_t)cap * N, stream));
+        CK(cudaMalloc(&p, 4 * (size_t)slots * N));
+        CK(cudaMemsetAsync(p, 0, 4 * (size_t)slots * N, stream));
         for (auto &a : allocs)
             if (a == (void *)nbr.idx) a = p;
         cudaFree(nbr.idx);
-        device_bytes += 4 * (size_t)(cap - list_cap_alloc) * N;
+        device_bytes += 4 * (size_t)(slots - list_cap_alloc) * N;
         nbr.idx = p;
-        list_cap_alloc = cap;
-        /* every captured step holds the old list pointer */
-        for (auto &g : graphs) {
-            if (g.exec) cudaGraphExecDestroy(g.exec);
-            if (g.graph) cudaGraphDestroy(g.graph);
-        }
-        graphs.clear();
+        list_cap_alloc = slots;
+        drop_graphs(); /* every captured step holds the old list pointer */
     }
-    nbr.cap = cap;
+    nbr.cap = slots;
     return FG_OK;
 }
 

@@ -21,6 +21,14 @@ void set_error_msg(const char *what);
 void fill_scene(FgScene &S, const fg_scene_desc &d);
 int validate(const fg_scene_desc &d);
 
+/* Element capacities of a world's buffers. */
+struct Capacity {
+    uint64_t particles = 0, buckets = 0, spheres = 0, bodies = 0, rb_buckets = 0, scenes = 0;
+    uint64_t work = 0, work_sph = 0; /* FG_CHUNK work items */
+    bool fits(const Capacity &o) const;
+    bool too_large() const;
+};
+
 struct World {
     /* layout */
     uint32_t nscenes = 0, n = 0, total_buckets = 0, nspheres = 0, nbodies = 0, total_rb_buckets = 0;
@@ -115,6 +123,15 @@ struct World {
     ~World();
     int alloc(void **p, size_t bytes);
     int create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st);
+    /* building blocks of create() that the server reuses */
+    Capacity cap;
+    static Capacity needs(const fg_scene_desc *d, uint32_t ns);
+    static size_t footprint(const Capacity &c, uint32_t list_cap);
+    int init_stream(cudaStream_t st);
+    int reserve(const Capacity &c);
+    int set_layout(const fg_scene_desc *d, uint32_t ns);
+    int upload_scene(uint32_t s, const fg_scene_desc &d);
+    void drop_graphs();
     Launch fluid_launch() const;
     Launch sphere_launch() const;
     uint32_t enqueue_step(cudaEvent_t *stage_events = nullptr);

@@ -246,6 +246,63 @@ int fg_probe_fp32_peak(float *tflops);
 int fg_sort_pairs_noalloc(unsigned int *keys, unsigned int *values, unsigned int keyBits, unsigned int n,
                           fg_stream_t stream);
 
+/* ---- served form: continuous batching of scenes (no reference
+ * counterpart; each scene's step is HeterogeneousSimulator::doTimeStep) ----
+ * Requests -- a scene and a step count -- queue on the host.  Every
+ * fg_server_step admits queued requests in arrival order while the resident
+ * scenes' device bytes stay within hbm_budget_bytes (and their particles
+ * within max_particles, if set), skipping requests that do not fit yet,
+ * advances every resident scene by one step in the same launches, and
+ * retires scenes that reached their step count (their final state is kept
+ * on the host until fg_server_result releases it).  A scene's result is the
+ * same bits as the scene stepped alone in a one-scene world. */
+typedef struct fg_server fg_server;
+typedef struct fg_server_config {
+    size_t hbm_budget_bytes;      /* device bytes the resident scenes may use */
+    uint32_t max_particles;       /* particles advanced per step, 0 = no limit */
+    uint32_t max_admit_per_step;  /* 0 = no limit */
+    int use_graphs;               /* replay captured steps while the resident set is stable */
+    int reserved[3];
+} fg_server_config;
+enum { FG_REQ_QUEUED = 0, FG_REQ_ACTIVE = 1, FG_REQ_DONE = 2 };
+typedef struct fg_server_step_info {
+    uint32_t active_scenes;   /* scenes advanced by this step */
+    uint32_t admitted;        /* of which newly admitted */
+    uint32_t finished;        /* scenes that reached their step count */
+    uint32_t queued;          /* requests still waiting */
+    uint64_t active_particles;
+    float step_ms;            /* device time of the step (CUDA events) */
+    float pad_;
+    double wall_ms;           /* host time of fg_server_step (admission, layout, step, retirement) */
+    size_t resident_bytes;
+} fg_server_step_info;
+typedef struct fg_request_info {
+    int state;                /* FG_REQ_* */
+    uint32_t steps_done, steps_total, n_particles;
+    double submit_s, admit_s, done_s; /* host clock, seconds since fg_server_create */
+    size_t resident_bytes;    /* budget charge while resident */
+} fg_request_info;
+typedef struct fg_server_stats_info {
+    uint64_t steps, particle_steps;
+    uint32_t queued, active;
+    size_t resident_bytes;    /* budget charge of the resident scenes */
+    uint64_t resident_particles;
+    size_t device_bytes;      /* bytes the server's world holds (capacity) */
+} fg_server_stats_info;
+void fg_server_config_defaults(fg_server_config *cfg); /* 120 GiB budget, graphs on */
+int fg_server_create(const fg_server_config *cfg, fg_stream_t stream, fg_server **out);
+void fg_server_destroy(fg_server *s);
+/* Copies the description and its arrays.  FG_E_BUDGET if the scene alone
+ * exceeds the budget. */
+int fg_server_submit(fg_server *s, const fg_scene_desc *scene, uint32_t steps, uint64_t *request_id);
+int fg_server_step(fg_server *s, fg_server_step_info *info);
+int fg_server_request(const fg_server *s, uint64_t request_id, fg_request_info *info);
+/* Final positions and velocities (n x float4 each, either may be NULL) of a
+ * finished request; release = 1 forgets the request.  FG_E_STATE if it has
+ * not finished. */
+int fg_server_result(fg_server *s, uint64_t request_id, float *pos4, float *vel4, int release);
+int fg_server_stats(const fg_server *s, fg_server_stats_info *stats);
+
 /* Small helpers so callers without a CUDA runtime binding can move data. */
 int fg_memcpy_d2h(void *dst, const void *src, size_t bytes);
 int fg_memcpy_h2d(void *dst, const void *src, size_t bytes);
