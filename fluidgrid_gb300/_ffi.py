@@ -66,7 +66,7 @@ class fg_scene_desc(ctypes.Structure):
 
 class fg_server_config(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_particles", c_u32), ("max_admit_per_step", c_u32),
-                ("use_graphs", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("use_graphs", ctypes.c_int), ("grow_via_host", ctypes.c_int), ("reserved", ctypes.c_int * 2)]
 
 
 class fg_server_step_info(ctypes.Structure):
@@ -102,7 +102,7 @@ STAGE_ALL = 255
 
 OPTIONS = {"neighbor_list": 1, "target_order": 2, "order_period": 3, "digit_bits": 4, "kernel": 5,
            "autotune_period": 6, "autotune_kernels": 7, "list_cap": 8, "ctas_per_sm": 10,
-           "autotune_tiles": 11, "list_autogrow": 12}
+           "autotune_tiles": 11, "list_autogrow": 12, "graph_steps": 13}
 NUM_KERNELS = 3
 
 STATUS = {0: "FG_OK", 1: "FG_E_INVALID", 2: "FG_E_CUDA", 3: "FG_E_OOM", 4: "FG_E_BUDGET", 5: "FG_E_NONFINITE",
@@ -117,7 +117,7 @@ C_ABI_SYMBOLS = [
     "fg_world_set_graphs", "fg_world_launches_per_step", "fg_world_stage_profile", "fg_world_timed_steps",
     "fg_world_e2e_steps", "fg_host_alloc", "fg_host_free", "fg_set_device", "fg_probe_fp32_peak",
     "fg_sort_pairs_noalloc", "fg_world_set_option", "fg_world_get_option", "fg_world_tuning_stats",
-    "fg_world_counters", "fg_world_list_overflows", "fg_server_config_defaults", "fg_server_create",
+    "fg_world_counters", "fg_world_list_overflows", "fg_world_timed_blocks", "fg_world_diagnostics", "fg_server_config_defaults", "fg_server_create",
     "fg_server_destroy", "fg_server_submit", "fg_server_step", "fg_server_request", "fg_server_result",
     "fg_server_stats",
     "fg_memcpy_d2h", "fg_memcpy_h2d",
@@ -172,6 +172,8 @@ def load():
     L.fg_world_set_graphs.argtypes = [VP, ctypes.c_int]
     L.fg_world_stage_profile.argtypes = [VP, ctypes.c_size_t, P(c_f)]
     L.fg_world_timed_steps.argtypes = [VP, c_u32, ctypes.c_size_t, P(c_f)]
+    L.fg_world_timed_blocks.argtypes = [VP, c_u32, c_u32, ctypes.c_size_t, P(c_f)]
+    L.fg_world_diagnostics.argtypes = [VP, P(ctypes.c_double)]
     L.fg_world_e2e_steps.argtypes = [VP, c_u32, VP, VP, VP, VP, P(c_f)]
     L.fg_host_alloc.argtypes = [ctypes.c_size_t]
     L.fg_host_alloc.restype = VP

@@ -76,6 +76,9 @@ int World::alloc(void **p, size_t bytes)
 World::~World()
 {
     if (flush_buf) cudaFree(flush_buf);
+    if (diag_first) cudaFree(diag_first);
+    if (diag_part) cudaFree(diag_part);
+    if (diag_out) cudaFree(diag_out);
     for (auto &e : tr.ev)
         if (e) cudaEventDestroy(e);
     for (auto &g : graphs) {
@@ -378,10 +381,13 @@ int World::set_layout(const fg_scene_desc *d, uint32_t ns)
         if (digit_bits > 8) digit_bits = 8;
     }
     std::vector<FgWork> fw, sw;
+    work_first_h.assign(ns + 1, 0);
     for (uint32_t s = 0; s < ns; s++) {
+        work_first_h[s] = (uint32_t)fw.size();
         build_work(fw, s, scenes_h[s].pbase, scenes_h[s].n);
         build_work(sw, s, scenes_h[s].sph_base, scenes_h[s].nsph);
     }
+    work_first_h[ns] = (uint32_t)fw.size();
     nwork = (uint32_t)fw.size();
     nwork_sph = (uint32_t)sw.size();
     single = (ns == 1);
@@ -696,9 +702,9 @@ int World::set_list_cap(uint32_t slots)
     return FG_OK;
 }
 
-int World::graph_for_current(cudaGraphExec_t *out)
+int World::graph_for_current(cudaGraphExec_t *out, uint32_t nsteps)
 {
-    const uint64_t sig = graph_signature();
+    const uint64_t sig = graph_signature() ^ ((uint64_t)(nsteps & 0xffu) << 56);
     for (auto &g : graphs)
         if (g.sig == sig) {
             *out = g.exec;
@@ -706,7 +712,7 @@ int World::graph_for_current(cudaGraphExec_t *out)
         }
     CachedGraph g{sig, nullptr, nullptr};
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_step();
+    for (uint32_t k = 0; k < nsteps; k++) enqueue_step();
     cudaError_t e = cudaStreamEndCapture(stream, &g.graph);
     if (e != cudaSuccess) {
         set_error("cudaStreamEndCapture", e);
@@ -802,9 +808,35 @@ int World::check_list_cap()
     return set_list_cap(want);
 }
 
+/* Steps at which the host acts between steps (autotuning rounds, list
+ * capacity checks): a multi-step graph never spans one. */
+bool World::host_boundary(uint64_t s) const
+{
+    if (tune_period && s % tune_period == 0) return true;
+    if (use_list && list_autogrow && s % FG_LIST_CHECK_PERIOD == 0) return true;
+    return false;
+}
+
 int World::step(uint32_t nsteps)
 {
     for (uint32_t k = 0; k < nsteps; k++) {
+        if (use_graphs && graph_steps > 1 && !tr.active && !use_order && nsteps - k >= graph_steps &&
+            !host_boundary(step_count)) {
+            bool clear = true;
+            for (uint32_t q = 1; q < graph_steps && clear; q++) clear = !host_boundary(step_count + q);
+            if (clear) {
+                /* graph_steps steps in one captured graph */
+                cudaGraphExec_t ge = nullptr;
+                int r = graph_for_current(&ge, graph_steps);
+                if (r != FG_OK) return r;
+                CK(cudaGraphLaunch(ge, stream));
+                tune_count[current_kernel()] += graph_steps;
+                counted_steps += graph_steps;
+                step_count += graph_steps;
+                k += graph_steps - 1;
+                continue;
+            }
+        }
         if (use_list && list_autogrow && step_count && (step_count % FG_LIST_CHECK_PERIOD == 0)) {
             int r = check_list_cap();
             if (r != FG_OK) return r;
@@ -871,6 +903,31 @@ __global__ void k_check(const float4 *pos, const float4 *vel, uint32_t n, uint32
             !isfinite(v.z))
             atomicOr(status, FG_DEV_NONFINITE);
     }
+}
+
+/* FP64 sums per scene (see fg_diag.cu); out: nscenes x FG_DIAG_COUNT. */
+int World::diagnostics(double *out)
+{
+    const size_t nw = std::max<uint32_t>(nwork, 1), ns = std::max<uint32_t>(nscenes, 1);
+    if (nw > diag_cap_work || ns > diag_cap_scenes) {
+        if (diag_first) cudaFree(diag_first);
+        if (diag_part) cudaFree(diag_part);
+        if (diag_out) cudaFree(diag_out);
+        diag_first = nullptr;
+        diag_part = diag_out = nullptr;
+        diag_cap_work = diag_cap_scenes = 0;
+        CK(cudaMalloc(&diag_first, 4 * (ns + 1)));
+        CK(cudaMalloc(&diag_part, 8 * 9 * nw));
+        CK(cudaMalloc(&diag_out, 8 * FG_DIAG_VALUES * ns));
+        diag_cap_work = nw;
+        diag_cap_scenes = ns;
+    }
+    if (!nscenes) return FG_OK;
+    CK(cudaMemcpyAsync(diag_first, work_first_h.data(), 4 * (nscenes + 1), cudaMemcpyHostToDevice, stream));
+    launch_diagnostics(fluid_launch(), nscenes, diag_first, pos, vel, bv, bL, bmass, diag_part, diag_out);
+    CK(cudaMemcpyAsync(out, diag_out, 8 * FG_DIAG_VALUES * (size_t)nscenes, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    return FG_OK;
 }
 
 int World::check()
@@ -943,7 +1000,7 @@ int World::stage_profile(size_t fbytes, float *ms)
     return FG_OK;
 }
 
-int World::timed_steps(uint32_t nsteps, size_t fbytes, float *ms)
+int World::timed_steps(uint32_t nsteps, size_t fbytes, float *ms, uint32_t per_block)
 {
     if (fbytes) {
         int r = ensure_flush(fbytes);
@@ -953,7 +1010,7 @@ int World::timed_steps(uint32_t nsteps, size_t fbytes, float *ms)
     for (uint32_t k = 0; k < nsteps; k++) {
         if (fbytes) launch_fill(flush_buf, fbytes / 4, k, stream);
         CK(cudaEventRecord(E.ev[2 * k], stream));
-        int r = step(1);
+        int r = step(per_block);
         if (r != FG_OK) return r;
         CK(cudaEventRecord(E.ev[2 * k + 1], stream));
     }
@@ -1306,6 +1363,10 @@ int fg_world_set_option(fg_world *w, int option, int value)
         return r;
     }
     case FG_OPT_LIST_AUTOGROW: W->list_autogrow = value != 0; return FG_OK;
+    case FG_OPT_GRAPH_STEPS:
+        if (value < 1 || value > 64) return FG_E_INVALID;
+        W->graph_steps = (uint32_t)value;
+        return FG_OK;
     case FG_OPT_CTAS_PER_SM:
         if (value < 0 || value > 64) return FG_E_INVALID;
         W->ctas_per_sm = (uint32_t)value;
@@ -1372,6 +1433,7 @@ int fg_world_get_option(const fg_world *w, int option, int *value)
     case FG_OPT_AUTOTUNE_KERNELS: *value = (int)W->tune_kernels; return FG_OK;
     case FG_OPT_LIST_CAP: *value = (int)W->nbr.cap; return FG_OK;
     case FG_OPT_LIST_AUTOGROW: *value = W->list_autogrow ? 1 : 0; return FG_OK;
+    case FG_OPT_GRAPH_STEPS: *value = (int)W->graph_steps; return FG_OK;
     case FG_OPT_CTAS_PER_SM: *value = (int)W->ctas_per_sm; return FG_OK;
     case FG_OPT_AUTOTUNE_TILES: *value = (int)W->tune_tiles; return FG_OK;
     default: return FG_E_INVALID;
@@ -1414,6 +1476,18 @@ int fg_world_timed_steps(fg_world *w, uint32_t nsteps, size_t flush_bytes, float
 {
     if (!w || (!ms && nsteps)) return FG_E_INVALID;
     return ((World *)w)->timed_steps(nsteps, flush_bytes, ms);
+}
+
+int fg_world_timed_blocks(fg_world *w, uint32_t nblocks, uint32_t steps_per_block, size_t flush_bytes, float *ms)
+{
+    if (!w || (!ms && nblocks) || !steps_per_block) return FG_E_INVALID;
+    return ((World *)w)->timed_steps(nblocks, flush_bytes, ms, steps_per_block);
+}
+
+int fg_world_diagnostics(fg_world *w, double *out)
+{
+    if (!w || !out) return FG_E_INVALID;
+    return ((World *)w)->diagnostics(out);
 }
 
 int fg_world_e2e_steps(fg_world *w, uint32_t nsteps, const float *host_pos4, const float *host_vel4,

@@ -87,7 +87,9 @@ struct World {
     };
     std::vector<CachedGraph> graphs;
     uint64_t graph_signature() const;
-    int graph_for_current(cudaGraphExec_t *out);
+    int graph_for_current(cudaGraphExec_t *out, uint32_t nsteps = 1);
+    uint32_t graph_steps = 1; /* steps per captured graph launch */
+    bool host_boundary(uint64_t s) const;
     /* online autotuner: every tune_period steps, each candidate value of one
      * tunable (kernel, block warps, digit width; the tunable rotates) runs
      * one real step under CUDA events and the fastest is kept */
@@ -132,6 +134,12 @@ struct World {
     int set_layout(const fg_scene_desc *d, uint32_t ns);
     int upload_scene(uint32_t s, const fg_scene_desc &d);
     void drop_graphs();
+    /* FP64 conservation diagnostics */
+    std::vector<uint32_t> work_first_h; /* scene s owns work items [first[s], first[s+1]) */
+    uint32_t *diag_first = nullptr;
+    double *diag_part = nullptr, *diag_out = nullptr;
+    size_t diag_cap_work = 0, diag_cap_scenes = 0;
+    int diagnostics(double *out);
     Launch fluid_launch() const;
     Launch sphere_launch() const;
     uint32_t enqueue_step(cudaEvent_t *stage_events = nullptr);
@@ -143,7 +151,7 @@ struct World {
     int sync();
     int ensure_flush(size_t bytes);
     int stage_profile(size_t flush_bytes, float *ms);
-    int timed_steps(uint32_t nsteps, size_t flush_bytes, float *ms);
+    int timed_steps(uint32_t nblocks, size_t flush_bytes, float *ms, uint32_t per_block = 1);
     int e2e_steps(uint32_t nsteps, const float *hp, const float *hv, float *op, float *ov, float *ms);
 };
 

@@ -162,6 +162,15 @@ void launch_segmented_sum(const float4 *in, const uint32_t *flags, float4 *out, 
 void launch_add_force_torque(const float4 *sum_f, const float4 *sum_t, const float4 *ordered_f, float4 *out_f,
                              float4 *out_t, const int *offsets, uint32_t nrb, cudaStream_t s);
 
+/* ---- FP64 conservation diagnostics (fg_diag.cu) ----
+ * out[scene * FG_DIAG_VALUES + q], q as the FG_DIAG_* enum of the public
+ * header; work_first[s]..work_first[s+1] are scene s's work items; part holds
+ * 9 doubles per work item. */
+#define FG_DIAG_VALUES 16 /* = FG_DIAG_COUNT of the public header */
+void launch_diagnostics(const Launch &L, uint32_t nscenes, const uint32_t *work_first, const float4 *pos,
+                        const float4 *vel, const FgD4 *bv, const FgD4 *bL, const double *bmass, double *part,
+                        double *out);
+
 /* L2 flush helper used by the benchmark */
 void launch_fill(uint32_t *buf, size_t words, uint32_t v, cudaStream_t s);
 

@@ -128,6 +128,8 @@ int Server::relayout()
     }
     const float4 *src_pos = nullptr, *src_vel = nullptr;
     const float2 *src_dp = nullptr;
+    std::vector<float4> host_pos, host_vel; /* growth through host memory */
+    std::vector<float2> host_dp;
     std::unique_ptr<World> nw;
     World *dst = w.get();
     const bool grow = !w || !w->cap.fits(need) || (need.bodies && !w->rb_local);
@@ -156,9 +158,29 @@ int Server::relayout()
             nw->ctas_per_sm = w->ctas_per_sm;
             nw->tune_period = w->tune_period;
             nw->use_graphs = w->use_graphs;
-            src_pos = w->pos;
-            src_vel = w->vel;
-            src_dp = w->dp;
+            size_t free_b = 0, total_b = 0;
+            CK(cudaMemGetInfo(&free_b, &total_b));
+            if (cfg.grow_via_host || World::footprint(c, nw->list_cap_alloc) + ((size_t)1 << 30) > free_b) {
+                /* both worlds would not fit at once: park the state on the
+                 * host, release the old world, then build the new one */
+                const size_t n0 = w->n;
+                host_pos.resize(n0);
+                host_vel.resize(n0);
+                host_dp.resize(n0);
+                if (n0) {
+                    CK(cudaMemcpy(host_pos.data(), w->pos, 16 * n0, cudaMemcpyDeviceToHost));
+                    CK(cudaMemcpy(host_vel.data(), w->vel, 16 * n0, cudaMemcpyDeviceToHost));
+                    CK(cudaMemcpy(host_dp.data(), w->dp, 8 * n0, cudaMemcpyDeviceToHost));
+                }
+                w.reset();
+                src_pos = host_pos.data();
+                src_vel = host_vel.data();
+                src_dp = host_dp.data();
+            } else {
+                src_pos = w->pos;
+                src_vel = w->vel;
+                src_dp = w->dp;
+            }
         }
         if ((r = nw->reserve(c)) != FG_OK) return r;
         dst = nw.get();
@@ -182,11 +204,11 @@ int Server::relayout()
         }
         const FgScene &O = old_scenes[it->second];
         if (S.n) {
-            CK(cudaMemcpyAsync(dst->pos + S.pbase, src_pos + O.pbase, 16 * (size_t)S.n, cudaMemcpyDeviceToDevice,
+            CK(cudaMemcpyAsync(dst->pos + S.pbase, src_pos + O.pbase, 16 * (size_t)S.n, cudaMemcpyDefault,
                                stream));
-            CK(cudaMemcpyAsync(dst->vel + S.pbase, src_vel + O.pbase, 16 * (size_t)S.n, cudaMemcpyDeviceToDevice,
+            CK(cudaMemcpyAsync(dst->vel + S.pbase, src_vel + O.pbase, 16 * (size_t)S.n, cudaMemcpyDefault,
                                stream));
-            CK(cudaMemcpyAsync(dst->dp + S.pbase, src_dp + O.pbase, 8 * (size_t)S.n, cudaMemcpyDeviceToDevice,
+            CK(cudaMemcpyAsync(dst->dp + S.pbase, src_dp + O.pbase, 8 * (size_t)S.n, cudaMemcpyDefault,
                                stream));
         }
         if (S.nbodies) {

@@ -62,6 +62,8 @@ class SceneSpec:
     ck: float = -10.0
     ckd: float = -5.0
     rb_rb: bool = False
+    rbrb_k: float = -10.0    # rigid/rigid contact spring and damping (the fluid/rigid values)
+    rbrb_kd: float = -5.0
     rb_gravity: tuple = (0.0, -9.8, 0.0, 0.0)
     rb_vlimit: float = 600.0
     name: str = "scene"
@@ -110,6 +112,7 @@ class SceneSpec:
         d.rb_to_fluid_relation[:] = list(self.r2f_rel)
         d.contact_kspring, d.contact_kdamping = self.ck, self.ckd
         d.rb_rb_contact = 1 if self.rb_rb else 0
+        d.rbrb_kspring, d.rbrb_kdamping = self.rbrb_k, self.rbrb_kd
         d.rb_gravity[:] = list(self.rb_gravity)
         d.rb_velocity_limit = self.rb_vlimit
         d.rb_dt = self.dt

@@ -163,6 +163,25 @@ class World:
         check(self.L.fg_world_timed_steps(self.h, int(nsteps), int(flush_bytes), ms), "fg_world_timed_steps")
         return np.array(ms[:nsteps], np.float64)
 
+    DIAG = ["active", "mass", "px", "py", "pz", "kinetic", "mx", "my", "mz", "body_px", "body_py", "body_pz",
+            "body_Lx", "body_Ly", "body_Lz", "body_kinetic"]
+
+    def diagnostics(self):
+        """FP64 conservation diagnostics computed on the GPU: one dict per
+        scene (fluid mass, momentum, kinetic energy, first moment; body
+        momentum, angular momentum, kinetic energy)."""
+        out = (ctypes.c_double * (16 * max(1, self.nscenes)))()
+        check(self.L.fg_world_diagnostics(self.h, out), "fg_world_diagnostics")
+        return [dict(zip(self.DIAG, out[16 * s:16 * s + 16])) for s in range(self.nscenes)]
+
+    def timed_blocks(self, nblocks, steps_per_block, flush_bytes=0):
+        """nblocks blocks of steps_per_block steps, each bracketed by CUDA
+        events; returns the block durations in ms."""
+        ms = (ctypes.c_float * max(1, nblocks))()
+        check(self.L.fg_world_timed_blocks(self.h, int(nblocks), int(steps_per_block), int(flush_bytes), ms),
+              "fg_world_timed_blocks")
+        return np.array(ms[:nblocks], np.float64)
+
     def e2e_steps(self, nsteps, host_pos, host_vel, out_pos, out_vel):
         ms = (ctypes.c_float * max(1, nsteps))()
         check(self.L.fg_world_e2e_steps(self.h, int(nsteps), _ptr(host_pos), _ptr(host_vel), _ptr(out_pos),

@@ -181,6 +181,9 @@ int fg_world_set_graphs(fg_world *w, int on);
  *                         it turns FG_OPT_LIST_AUTOGROW off)
  *   FG_OPT_LIST_AUTOGROW  kernel 1: 1 = every 25 steps grow the capacity to
  *                         1.125x the largest in-range count seen (default)
+ *   FG_OPT_GRAPH_STEPS    steps captured in one CUDA graph launch (1..64,
+ *                         default 1); such a launch never spans an
+ *                         autotuning round or a list capacity check
  *   FG_OPT_CTAS_PER_SM    kernels 0/1: CTAs per SM of the persistent
  *                         128-thread density/force grids (0 = 16)
  *   FG_OPT_AUTOTUNE_TILES bit mask of the tunables the autotuner varies:
@@ -192,7 +195,7 @@ int fg_world_set_graphs(fg_world *w, int on);
 enum {
     FG_OPT_NEIGHBOR_LIST = 1, FG_OPT_TARGET_ORDER = 2, FG_OPT_ORDER_PERIOD = 3, FG_OPT_DIGIT_BITS = 4,
     FG_OPT_KERNEL = 5, FG_OPT_AUTOTUNE_PERIOD = 6, FG_OPT_AUTOTUNE_KERNELS = 7, FG_OPT_LIST_CAP = 8,
-    FG_OPT_CTAS_PER_SM = 10, FG_OPT_AUTOTUNE_TILES = 11, FG_OPT_LIST_AUTOGROW = 12
+    FG_OPT_CTAS_PER_SM = 10, FG_OPT_AUTOTUNE_TILES = 11, FG_OPT_LIST_AUTOGROW = 12, FG_OPT_GRAPH_STEPS = 13
 };
 #define FG_NUM_KERNELS 3
 int fg_world_set_option(fg_world *w, int option, int value);
@@ -220,6 +223,24 @@ int fg_world_stage_profile(fg_world *w, size_t flush_bytes, float stage_ms[8]);
  * flush_bytes buffer is rewritten so no step starts with a warm L2.
  * ms[k] = duration of step k. */
 int fg_world_timed_steps(fg_world *w, uint32_t nsteps, size_t flush_bytes, float *ms);
+/* FP64 conservation diagnostics, per scene FG_DIAG_COUNT doubles summed on
+ * the GPU in a fixed order (reproducible bit for bit): out[scene *
+ * FG_DIAG_COUNT + q].  Synchronises the world's stream. */
+enum {
+    FG_DIAG_ACTIVE = 0,         /* active particles (w > 0) */
+    FG_DIAG_MASS = 1,           /* sum m */
+    FG_DIAG_MOMENTUM = 2,       /* sum m v (3) */
+    FG_DIAG_KINETIC = 5,        /* sum m |v|^2 / 2 */
+    FG_DIAG_MOMENT = 6,         /* sum m x (3): centre of mass times mass */
+    FG_DIAG_BODY_MOMENTUM = 9,  /* sum M v of the bodies (3) */
+    FG_DIAG_BODY_ANGULAR = 12,  /* sum L of the bodies (3) */
+    FG_DIAG_BODY_KINETIC = 15,  /* sum M |v|^2 / 2 of the bodies */
+    FG_DIAG_COUNT = 16
+};
+int fg_world_diagnostics(fg_world *w, double *out);
+/* nblocks blocks of steps_per_block steps each (multi-step graphs apply),
+ * each block bracketed by events; ms[k] = duration of block k. */
+int fg_world_timed_blocks(fg_world *w, uint32_t nblocks, uint32_t steps_per_block, size_t flush_bytes, float *ms);
 /* End to end through host memory: per step, copy positions and velocities
  * from host_pos4/host_vel4 to the device, step, copy them back to
  * out_pos4/out_vel4; ms[k] = device time of step k including both copies.
@@ -262,7 +283,9 @@ typedef struct fg_server_config {
     uint32_t max_particles;       /* particles advanced per step, 0 = no limit */
     uint32_t max_admit_per_step;  /* 0 = no limit */
     int use_graphs;               /* replay captured steps while the resident set is stable */
-    int reserved[3];
+    int grow_via_host;            /* 1: when the world grows, always park the state on the host
+                                     (otherwise only when both worlds would not fit) */
+    int reserved[2];
 } fg_server_config;
 enum { FG_REQ_QUEUED = 0, FG_REQ_ACTIVE = 1, FG_REQ_DONE = 2 };
 typedef struct fg_server_step_info {

@@ -45,10 +45,10 @@ def _run(server, ss, steps, arrive):
     return ids, max_active
 
 
-@pytest.mark.parametrize("graphs", [True, False])
-def test_results_equal_scene_alone(graphs):
+@pytest.mark.parametrize("graphs,via_host", [(True, False), (False, False), (True, True)])
+def test_results_equal_scene_alone(graphs, via_host):
     ss, steps, arrive = _mix()
-    with Server(budget_bytes=64 << 30, use_graphs=graphs) as srv:
+    with Server(budget_bytes=64 << 30, use_graphs=graphs, grow_via_host=via_host) as srv:
         ids, max_active = _run(srv, ss, steps, arrive)
         assert max_active >= 3  # the scenes really overlapped on the device
         for s, rid in ids.items():
