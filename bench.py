@@ -216,6 +216,104 @@ def run_reference(args, rank, world):
     return 0
 
 
+def pct(a, q):
+    return float(np.percentile(np.asarray(a, np.float64), q)) if len(a) else None
+
+
+def run_batched(steps=1000, warmup=10, plain_sample=64):
+    """Batched form: 256 uneven scenes (2,048-65,536 particles, half with a
+    rigid sphere) in one world -- one segment-aware launch per stage, ten
+    steps per captured graph -- against the plain path that steps each scene
+    in its own one-scene world, one scene after another (timed on every
+    4th scene, the rest by the same per-particle rate)."""
+    from fluidgrid_gb300 import scenes
+    from fluidgrid_gb300.world import World
+    ss = scenes.batched_scenes(count=256)
+    N = sum(s.n for s in ss)
+    w = World(ss)
+    w.set_option("graph_steps", 10)
+    w.step(warmup)
+    w.sync()
+    blocks = w.timed_blocks(steps // 10, 10)
+    w.check_finite()
+    per_step = w.timed_steps(50)  # one step per graph: per-step latency of every scene in the batch
+    tuning = w.tuning_stats()
+    diag = w.diagnostics()
+    w.close()
+    total_ms = float(blocks.sum())
+    value = N * (steps // 10) * 10 / (total_ms * 1e-3)
+    # plain path: each scene alone, sequentially
+    sample = ss[::max(1, len(ss) // plain_sample)]
+    t_plain, n_plain = 0.0, 0
+    for sp in sample:
+        ws = World([sp])
+        ws.step(3)
+        ms = ws.timed_steps(10)
+        ws.close()
+        t_plain += float(np.mean(ms))
+        n_plain += sp.n
+    plain = n_plain / (t_plain * 1e-3)
+    return {"workload": "batched_256", "scenes": len(ss), "particles": N,
+            "rigid_spheres": sum(s.nspheres for s in ss), "steps": (steps // 10) * 10,
+            "value": value, "unit": "particle-steps/s", "ms_per_step": total_ms / ((steps // 10) * 10),
+            "graph_steps": 10, "scene_step_latency_ms": {"p50": pct(per_step, 50), "p99": pct(per_step, 99)},
+            "plain_sequential": {"value": plain, "unit": "particle-steps/s", "scenes_timed": len(sample)},
+            "speedup_vs_plain": value / plain,
+            "fp64_mass_total": float(sum(d["mass"] for d in diag)),
+            "l2": "inputs larger than L2 (%.0f MB of particle state)" % (N * 32 / 1e6),
+            "autotune": tuning}
+
+
+def run_served(duration=20.0, rate=200.0, budget=120 << 30, max_particles=0, seed=0x5EED, label="served"):
+    """Served form: Poisson arrivals of dam-break requests (fluid counts
+    log-uniform in [4,096, 524,288], 0-4 rigid boxes of 1,024 spheres, step
+    counts uniform in [100, 2000]) for `duration` seconds of wall time into a
+    continuous-batching server with an HBM budget; every server step admits
+    what fits and advances every resident scene."""
+    from fluidgrid_gb300 import scenes
+    from fluidgrid_gb300.server import Server
+    pool = scenes.served_templates(seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, int(rate * duration * 1.5) + 16))
+    arrivals = arrivals[arrivals < duration]
+    picks = rng.integers(0, len(pool), len(arrivals))
+    nsteps = rng.integers(100, 2001, len(arrivals))
+    srv = Server(budget_bytes=budget, max_particles=max_particles)
+    ids = []
+    infos = []
+    t0 = time.perf_counter()
+    k = 0
+    while True:
+        now = time.perf_counter() - t0
+        if now >= duration:
+            break
+        while k < len(arrivals) and arrivals[k] <= now:
+            ids.append(srv.submit(pool[picks[k]], int(nsteps[k])))
+            k += 1
+        infos.append(srv.step())
+    elapsed = time.perf_counter() - t0
+    st = srv.stats()
+    reqs = [srv.request(i) for i in ids]
+    srv.close()
+    done = [r for r in reqs if r["state"] == 2]
+    admitted = [r for r in reqs if r["state"] >= 1]
+    step_ms = [i["step_ms"] for i in infos if i["active_particles"]]
+    wall_ms = [i["wall_ms"] for i in infos if i["active_particles"]]
+    return {"workload": label, "duration_s": duration, "arrival_rate_per_s": rate, "budget_bytes": budget,
+            "max_particles_per_step": max_particles, "submitted": len(ids), "admitted": len(admitted),
+            "completed": len(done), "queued_at_end": st["queued"], "server_steps": st["steps"],
+            "value": st["particle_steps"] / elapsed, "unit": "particle-steps/s",
+            "step_latency_ms": {"p50": pct(step_ms, 50), "p99": pct(step_ms, 99)},
+            "server_step_wall_ms": {"p50": pct(wall_ms, 50), "p99": pct(wall_ms, 99)},
+            "request_latency_s": {"p50": pct([r["done_s"] - r["submit_s"] for r in done], 50),
+                                  "p99": pct([r["done_s"] - r["submit_s"] for r in done], 99)},
+            "admission_wait_s": {"p50": pct([r["admit_s"] - r["submit_s"] for r in admitted], 50),
+                                 "p99": pct([r["admit_s"] - r["submit_s"] for r in admitted], 99)},
+            "max_resident_particles": int(max([i["active_particles"] for i in infos] + [0])),
+            "max_resident_bytes": int(max([i["resident_bytes"] for i in infos] + [0])),
+            "device_bytes": st["device_bytes"]}
+
+
 def run_ours(args, rank, world, local):
     import fluidgrid_gb300 as fgm
     from fluidgrid_gb300.world import World, PinnedArray, fp32_peak_tflops
@@ -275,6 +373,15 @@ def run_ours(args, rank, world, local):
     stages = {key: float(np.mean([p[key] for p in prof])) for key in prof[0]} if prof else {}
     value = world * n * K / (total_ms * 1e-3)
     e2e_value = world * n * K / (e2e_ms * 1e-3)
+    # 4. the batched and served forms (one GPU each rank, replicas)
+    forms = {}
+    if "batched" in args.forms:
+        forms["batched"] = run_batched()
+    if "served" in args.forms:
+        forms["served"] = run_served(duration=args.served_seconds)
+        # latency-bounded serving: at most 1M particles advanced per step
+        forms["served_latency"] = run_served(duration=args.served_seconds / 2, max_particles=1_000_000,
+                                             label="served_latency_bounded")
     if rank == 0:
         peak, peak_kind = measured_peaks()
         dom = max(("forces", "density"), key=lambda k: stages.get(k, 0.0))
@@ -311,6 +418,7 @@ def run_ours(args, rank, world, local):
                     "d2h_bytes_per_step": 32 * n},
             "gpu_launches": launches * K + K,
             "clocks": clk,
+            "forms": forms,
         }
         print(json.dumps(line))
     dist.close()
@@ -326,6 +434,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="dam_break_rigid_1m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--forms", default="batched,served",
+                    help="comma list of extra forms to measure after the plain path: batched, served")
+    ap.add_argument("--served-seconds", type=float, default=20.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -148,10 +148,15 @@ int Server::relayout()
             c.work = g(need.work, w->cap.work);
             c.work_sph = g(need.work_sph, w->cap.work_sph);
         }
-        if (c.too_large()) c = need;
+        const uint32_t lc = w ? w->list_cap_alloc : FG_LIST_CAP_DEFAULT;
+        /* headroom only while the world stays within the budget */
+        if (c.too_large() || World::footprint(c, lc) > cfg.hbm_budget_bytes) c = need;
         nw.reset(new World());
         int r = nw->init_stream(stream);
         if (r != FG_OK) return r;
+        /* the budget charges list memory at the admission-time capacity: the
+         * lists do not grow (denser particles walk their buckets instead) */
+        nw->list_autogrow = false;
         if (w) {
             nw->list_cap_alloc = w->list_cap_alloc;
             nw->digit_bits = w->digit_bits;

@@ -281,6 +281,41 @@ def batched_scenes(seed=0x5EED, count=256, nmin=2048, nmax=65536):
     return out
 
 
+def dam_break_request(n, nboxes, rng, name="request"):
+    """A served-form request: a dam-break block of n particles (jittered
+    lattice at 0.5h) in a walled box of twice the block's footprint, with
+    `nboxes` rigid boxes of side 0.2 m (1,024 surface spheres, 10 kg each)
+    dropped from above the block at seeded poses."""
+    nx = max(4, int(round((n / 2.0) ** (1.0 / 3.0) * 1.26)))
+    nz = nx
+    ny = max(2, int(math.ceil(n / (nx * nz))))
+    pos = lattice(nx, ny, nz, SPACING, (SPACING, SPACING, SPACING), 0.05 * H, rng)[:n]
+    ext = np.array([nx, ny, nz], np.float64) * SPACING + 2 * SPACING
+    box = (float(ext[0] * 1.4142), float(max(ext[1] * 2.0, 0.8)), float(ext[2] * 1.4142))
+    bodies = []
+    for b in range(nboxes):
+        c = (float(rng.uniform(0.15, box[0] - 0.15)), float(ext[1] + 0.2 + 0.25 * b),
+             float(rng.uniform(0.15, box[2] - 0.15)))
+        bodies.append(Body(local=box_surface(0.2, 1024, rng), mass=10.0, position=c,
+                           orientation=random_quaternion(rng)))
+    nb = next_pow2(max(n, 4096))
+    return SceneSpec(pos=pos, box_min=(0, 0, 0), box_max=box, buckets=(nb, 1, 1), bodies=bodies,
+                     rb_buckets=(8192, 1, 1), name=name)
+
+
+def served_templates(seed=0x5EED, count=24, nmin=4096, nmax=524288):
+    """Scene pool of the served workload: fluid counts log-uniform in
+    [nmin, nmax], 0-4 rigid boxes each.  Requests draw from this pool (with
+    their own step counts) so that generating scenes on the host does not
+    pace the arrival process."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+        out.append(dam_break_request(n, int(rng.integers(0, 5)), rng, name="served_%d" % s))
+    return out
+
+
 WORKLOADS = {
     "dam_break_16k": dam_break_small,
     "dam_break_rigid_1m": dam_break_rigid,
