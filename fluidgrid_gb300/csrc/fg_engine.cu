@@ -172,7 +172,7 @@ int validate(const fg_scene_desc &d)
         if (rnb > 0x7fffffffLL) return FG_E_INVALID;
         for (uint32_t b = 0; b < d.n_bodies; b++) {
             if (d.bodies[b].n_spheres && !d.bodies[b].local_spheres) return FG_E_INVALID;
-            if (!(d.bodies[b].mass != 0.0f)) return FG_E_INVALID;
+            if (!(d.bodies[b].mass >= 0.0f)) return FG_E_INVALID; /* 0 = static body */
         }
     }
     return FG_OK;

@@ -246,7 +246,9 @@ __global__ void __launch_bounds__(BODY_THREADS) k_body_update(const FgScene *__r
                 }
             st.force_sum[b] = fg_d4(F[0], F[1], F[2], F[3]);
             st.torque_sum[b] = fg_d4(T[0], T[1], T[2], T[3]);
-            if (integrate) {
+            /* mass 0: a static body (the reference's "static" rigid-body
+             * file type), never integrated */
+            if (integrate && st.mass[b] != 0.0) {
                 const FgScene *S = table ? table + body_scene[b] : &single;
                 /* IntegrateRBK in double */
                 const double vl = S->rb_vlimit;

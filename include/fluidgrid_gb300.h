@@ -46,7 +46,7 @@ typedef enum fg_status {
 typedef struct fg_body_desc {
     uint32_t n_spheres;
     const float *local_spheres; /* host float4[n_spheres]: x,y,z (w ignored) */
-    float mass;
+    float mass;            /* 0 = static body: never integrated (contact at zero velocity) */
     float position[3];     /* centre of mass */
     float orientation[4];  /* quaternion x,y,z,w */
     float inv_inertia[9];  /* row-major body-frame inverse inertia */

@@ -116,7 +116,7 @@ def test_invalid_scene_rejected_without_gpu(lib):
     st, _, _ = _create(lib, spec)
     assert _ffi.STATUS[st] == "FG_E_INVALID"
     spec = scenes.dam_break_rigid(nx=8, ny=4, nz=8, spheres=64)
-    spec.bodies[0].mass = 0.0
+    spec.bodies[0].mass = -1.0  # 0 is a static body; negative is invalid
     st, _, _ = _create(lib, spec)
     assert _ffi.STATUS[st] == "FG_E_INVALID"
 
