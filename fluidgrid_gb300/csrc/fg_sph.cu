@@ -33,18 +33,6 @@
 
 namespace fg {
 
-/* Kahan-compensated accumulator */
-struct Kahan {
-    float s, c;
-    __device__ __forceinline__ void add(float x)
-    {
-        float y = x - c;
-        float t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
-};
-
 template <bool LIST>
 __global__ void __launch_bounds__(FG_CHUNK, 8) k_density(const FgWork *__restrict__ work, uint32_t nwork,
                                                      uint32_t n_single, const FgScene *__restrict__ table,
@@ -69,47 +57,21 @@ __global__ void __launch_bounds__(FG_CHUNK, 8) k_density(const FgWork *__restric
         const uint32_t i = (ord.tord && valid) ? __ldg(ord.inv + __ldg(ord.tord + tpos)) : tpos;
         const float4 p = valid ? spos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const bool active = valid && p.w > 0.0f; /* inactive: density not written */
-        uint32_t cnt = 0, dcnt = 0; /* list entries; density visits */
-        /* the last list entries not yet stored (stored four at a time) */
-        uint32_t q0 = 0, q1 = 0, q2 = 0, q3 = 0;
+        DensityAcc acc;
+        acc.init();
         uint32_t *lp = LIST ? list.idx + (size_t)tpos * list.cap : nullptr;
         if (active) {
             const float scale = S->scale, h2 = S->h2;
             const float px = p.x * scale, py = p.y * scale, pz = p.z * scale;
-            Kahan acc = {0.f, 0.f};
+            const uint32_t cap = LIST ? list.cap : 0u;
             fg_walk27(p.x, p.y, p.z, S, start, end, [&](uint32_t j) {
-                const float4 q = __ldg(spos + j);
-                const float dx = fmaf(-q.x, scale, px), dy = fmaf(-q.y, scale, py), dz = fmaf(-q.z, scale, pz);
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                if (r2 <= h2) {
-                    /* l < h adds (h^2 - l^2)^3; at l = h that is an exact 0 */
-                    const float t = h2 - r2;
-                    acc.add(t * t * t);
-                    dcnt++;
-                    /* the force pass's neighbours (l <= h, not itself) */
-                    if (LIST && j != i) {
-                        q0 = q1;
-                        q1 = q2;
-                        q2 = q3;
-                        q3 = j;
-                        cnt++;
-                        if ((cnt & 3u) == 0u && cnt <= list.cap)
-                            *reinterpret_cast<uint4 *>(lp + cnt - 4u) = make_uint4(q0, q1, q2, q3);
-                    }
-                }
+                acc.visit<LIST>(__ldg(spos + j), j, px, py, pz, scale, h2, i, lp, cap);
             });
-            if (LIST && (cnt & 3u) && cnt < list.cap) {
-                /* the last 1..3 entries sit in q3, (q2, q3) or (q1, q2, q3) */
-                const uint32_t r = cnt & 3u;
-                const uint4 t = r == 1u ? make_uint4(q3, 0u, 0u, 0u)
-                                        : (r == 2u ? make_uint4(q2, q3, 0u, 0u) : make_uint4(q1, q2, q3, 0u));
-                *reinterpret_cast<uint4 *>(lp + (cnt & ~3u)) = t;
-            }
+            if (LIST) acc.flush(lp, cap);
             const float mass = use_o ? mass_o : S->mass;
             const float gas = use_o ? gas_o : S->gas;
             const float rest = use_o ? rest_o : S->rest;
-            const float rho = (mass * S->kpoly6) * acc.s;
-            const float2 d = make_float2(fmaxf(1.0f, rho), gas * (rho - rest));
+            const float2 d = fg_density_out(mass, S->kpoly6, gas, rest, acc.s);
             dp[i] = d;
             if (LIST) {
                 const float4 v = __ldg(svel + i);
@@ -123,6 +85,7 @@ __global__ void __launch_bounds__(FG_CHUNK, 8) k_density(const FgWork *__restric
             list.rec[2 * i] = make_float4(p.x, p.y, p.z, d.x);
             list.rec[2 * i + 1] = make_float4(v.x, v.y, v.z, d.y);
         }
+        const uint32_t cnt = acc.cnt, dcnt = acc.dcnt;
         if (LIST && valid) list.cnt[tpos] = cnt;
         pc += dcnt;
         mx = max(mx, cnt);

@@ -38,9 +38,74 @@ __device__ __forceinline__ void fg_walk27(float px, float py, float pz, const Fg
             const uint32_t st = fg_sel3(s0, s1, s2, x);
             if (st == FG_EMPTY) continue; /* end of an empty bucket is stale */
             const uint32_t en = fg_sel3(e0, e1, e2, x);
+#pragma unroll 2
             for (uint32_t j = st; j < en; j++) fn(j);
         }
     }
+}
+
+/* One target's state in a density pass: the Kahan sum of (h^2 - l^2)^3 over
+ * the candidates with l <= h (an exact 0 at l = h, so the sum equals the
+ * reference's l < h sum) and the force pass's neighbour list (l <= h, not
+ * the target itself), buffered in registers and stored four entries at a
+ * time.  Every operation is rounded on its own, so any kernel that visits the
+ * same candidates in the same order produces the same bits. */
+struct DensityAcc {
+    float s, c;          /* Kahan sum and compensation */
+    uint32_t dcnt, cnt;  /* density visits, list entries */
+    uint32_t q0, q1, q2, q3; /* the last list entries not yet stored */
+
+    __device__ __forceinline__ void init()
+    {
+        s = c = 0.0f;
+        dcnt = cnt = 0;
+        q0 = q1 = q2 = q3 = 0;
+    }
+
+    template <bool LIST>
+    __device__ __forceinline__ void visit(float4 q, uint32_t j, float px, float py, float pz, float scale, float h2,
+                                          uint32_t self, uint32_t *lp, uint32_t cap)
+    {
+        const float dx = fmaf(-q.x, scale, px), dy = fmaf(-q.y, scale, py), dz = fmaf(-q.z, scale, pz);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
+        if (r2 <= h2) {
+            const float t = __fsub_rn(h2, r2);
+            const float x = __fmul_rn(__fmul_rn(t, t), t);
+            const float y = __fsub_rn(x, c);
+            const float u = __fadd_rn(s, y);
+            c = __fsub_rn(__fsub_rn(u, s), y);
+            s = u;
+            dcnt++;
+            if (LIST && j != self) {
+                q0 = q1;
+                q1 = q2;
+                q2 = q3;
+                q3 = j;
+                cnt++;
+                if ((cnt & 3u) == 0u && cnt <= cap)
+                    *reinterpret_cast<uint4 *>(lp + cnt - 4u) = make_uint4(q0, q1, q2, q3);
+            }
+        }
+    }
+
+    /* store the last 1..3 entries (they sit in q3, (q2, q3) or (q1, q2, q3)) */
+    __device__ __forceinline__ void flush(uint32_t *lp, uint32_t cap) const
+    {
+        if ((cnt & 3u) && cnt < cap) {
+            const uint32_t r = cnt & 3u;
+            const uint4 t = r == 1u ? make_uint4(q3, 0u, 0u, 0u)
+                                    : (r == 2u ? make_uint4(q2, q3, 0u, 0u) : make_uint4(q1, q2, q3, 0u));
+            *reinterpret_cast<uint4 *>(lp + (cnt & ~3u)) = t;
+        }
+    }
+};
+
+/* CalculateMassDensityK's output (K_FluidSim.cu:244-251): (max(1, rho),
+ * k (rho - rho0)) with rho = m kPoly6 sum, each operation rounded alone. */
+__device__ __forceinline__ float2 fg_density_out(float mass, float kpoly6, float gas, float rest, float sum)
+{
+    const float rho = __fmul_rn(__fmul_rn(mass, kpoly6), sum);
+    return make_float2(fmaxf(1.0f, rho), __fmul_rn(gas, __fsub_rn(rho, rest)));
 }
 
 /* scene owning a global bucket key (scenes are ordered by bucket_base) */

@@ -49,8 +49,11 @@ def _variants():
 VARIANTS = _variants()
 
 
-def _step(spec, fused=True, vel0=None, digit_bits=None, graphs=True):
+def _step(spec, fused=True, vel0=None, digit_bits=None, graphs=True, kernel=None):
     w = World([spec])
+    if kernel is not None:
+        w.set_option("autotune_period", 0)
+        w.set_option("kernel", kernel)
     w.set_fused_integrate(fused)
     w.set_graphs(graphs)
     if digit_bits:
@@ -168,6 +171,7 @@ def test_tunables_do_not_change_results(name):
         for order in (0, 1):
             for period in ((1, 16) if order else (16,)):
                 w = World([spec])
+                w.set_option("autotune_period", 0)
                 w.set_option("kernel", kernel)
                 w.set_option("target_order", order)
                 w.set_option("order_period", period)
@@ -358,13 +362,14 @@ def test_each_kernel_matches_oracle(kernel):
     _forces_check(spec, spec.pos, v0, g)
 
 
-def test_cell_cooperative_kernel_dense_runs():
+@pytest.mark.parametrize("kernel", [1, 2])
+def test_dense_runs(kernel):
     """Runs longer than a warp (dense buckets) and candidate sets larger than
     the shared-memory stage: a compressed block with 4x the lattice density."""
     rng = np.random.default_rng(8)
     pos = lattice(24, 12, 24, SPACING * 0.5, (0.2, 0.2, 0.2), 0.02 * H, rng)
     spec = SceneSpec(pos=pos, buckets=(32, 32, 32), name="dense")
-    pos0, v0, g = _step(spec)
+    pos0, v0, g = _step(spec, kernel=kernel)
     ref = T.oracle_grid(spec, pos0, v0)
     occ = ref["start"] != 0xFFFFFFFF
     assert (ref["end"][occ].astype(np.int64) - ref["start"][occ]).max() > 32
