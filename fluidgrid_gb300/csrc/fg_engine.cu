@@ -239,7 +239,7 @@ size_t World::footprint(const Capacity &c, uint32_t list_cap)
     if (c.bodies) {
         b += S * (16 * 6 + 12);
         b += 8 * std::max<uint64_t>(c.rb_buckets, 1);
-        b += c.bodies * (32 * 6 + 16 * 3 + 8 + 72 + 12);
+        b += c.bodies * (32 * 6 + 16 * 3 + 8 + 72 + 12 + 8 * 8 * FG_BODY_CHUNKS);
     }
     return b;
 }
@@ -313,6 +313,7 @@ int World::reserve(const Capacity &c)
         if ((r = A((void **)&bq, 32 * B))) return r;
         if ((r = A((void **)&bL, 32 * B))) return r;
         if ((r = A((void **)&bfs, 32 * B))) return r;
+        if ((r = A((void **)&body_part, 8 * 8 * FG_BODY_CHUNKS * B))) return r;
         if ((r = A((void **)&bts, 32 * B))) return r;
         if ((r = A((void **)&bxf, 16 * B))) return r;
         if ((r = A((void **)&bvf, 16 * B))) return r;
@@ -652,6 +653,7 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         b.mass = bmass;
         b.x_f = bxf; b.v_f = bvf; b.q_f = bqf;
         b.force_sum = bfs; b.torque_sum = bts;
+        b.partial = body_part;
         launch_body_update(single ? nullptr : scenes_d, &scenes_h[0], body_scene, body_first, body_count, nbodies,
                            rb_force, rb_torque, b, 1, stream);
         mark(7, 1);

@@ -67,6 +67,7 @@ struct World {
     uint32_t *rb_keys_u = nullptr, *rb_keys = nullptr, *rb_ids = nullptr, *rb_start = nullptr, *rb_end = nullptr;
     int *aabb = nullptr;
     FgD4 *bx = nullptr, *bv = nullptr, *bq = nullptr, *bL = nullptr, *bfs = nullptr, *bts = nullptr;
+    double *body_part = nullptr; /* FG_BODY_CHUNKS x 8 FP64 partial sums per body */
     float4 *bxf = nullptr, *bvf = nullptr, *bqf = nullptr;
     double *bmass = nullptr, *binv = nullptr;
     uint32_t *body_scene = nullptr, *body_first = nullptr, *body_count = nullptr;

@@ -141,10 +141,13 @@ struct BodyState {
     const double *mass;
     float4 *x_f, *v_f, *q_f; /* FP32 mirrors read by the contact kernels */
     FgD4 *force_sum, *torque_sum; /* FP64 per-body sums (diagnostic output) */
+    double *partial;              /* FG_BODY_CHUNKS x 8 FP64 partial sums per body, or null */
 };
 
 /* Per body: FP64 sum of its spheres' force/torque (unsorted, body-contiguous
- * sphere ranges) followed by the FP64 body integrator. */
+ * sphere ranges) followed by the FP64 body integrator.  With st.partial the
+ * sum is spread over FG_BODY_CHUNKS CTAs per body and added in a fixed order. */
+#define FG_BODY_CHUNKS 16
 void launch_body_update(const FgScene *table, const FgScene *single, const uint32_t *body_scene,
                         const uint32_t *body_first, const uint32_t *body_count, uint32_t nbodies,
                         const float4 *force, const float4 *torque, BodyState st, int integrate, cudaStream_t s);

@@ -19,62 +19,74 @@
 namespace fg {
 
 /* Contact sum of one rigid sphere against the fluid grid, then force and
- * torque written at the sphere's unsorted index (body-contiguous). */
-__global__ void __launch_bounds__(FG_CHUNK) k_rb_from_fluid(const FgWork *__restrict__ work, uint32_t nwork,
-                                                           uint32_t n_single, const FgScene *__restrict__ table,
-                                                           const __grid_constant__ FgScene single,
-                                                           const float4 *__restrict__ rb_spos,
-                                                           const uint32_t *__restrict__ rb_ids,
-                                                           const float4 *__restrict__ body_vel,
-                                                           const float4 *__restrict__ body_cm,
-                                                           const float4 *__restrict__ fl_spos,
-                                                           const float4 *__restrict__ fl_svel,
-                                                           const uint32_t *__restrict__ fl_start,
-                                                           const uint32_t *__restrict__ fl_end,
-                                                           float4 *__restrict__ force, float4 *__restrict__ torque,
-                                                           int add)
+ * torque written at the sphere's unsorted index (body-contiguous).  One warp
+ * per sphere, so a few thousand spheres still fill the GPU: the lanes take
+ * the (2r+1)^3 fluid buckets in turn and a fixed shuffle tree adds their
+ * partial sums (deterministic; the FP32 terms are the reference's, their
+ * summation order differs).  CTA = RBF_WARPS warps; CTA c takes spheres
+ * RBF_WARPS (c % 32) + warp of work item c / 32. */
+#define RBF_WARPS 4
+__global__ void __launch_bounds__(RBF_WARPS * 32) k_rb_from_fluid(const FgWork *__restrict__ work, uint32_t nwork,
+                                                                 uint32_t n_single, const FgScene *__restrict__ table,
+                                                                 const __grid_constant__ FgScene single,
+                                                                 const float4 *__restrict__ rb_spos,
+                                                                 const uint32_t *__restrict__ rb_ids,
+                                                                 const float4 *__restrict__ body_vel,
+                                                                 const float4 *__restrict__ body_cm,
+                                                                 const float4 *__restrict__ fl_spos,
+                                                                 const float4 *__restrict__ fl_svel,
+                                                                 const uint32_t *__restrict__ fl_start,
+                                                                 const uint32_t *__restrict__ fl_end,
+                                                                 float4 *__restrict__ force,
+                                                                 float4 *__restrict__ torque, int add)
 {
-    for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
-        FgWork it = fg_work(work, w, n_single);
-        if (threadIdx.x >= it.count) continue;
-        const FgScene *S = fg_scene(table, &single, it.scene);
-        const uint32_t i = it.first + threadIdx.x;
-        const float4 p = rb_spos[i];
-        const int b = (int)p.w;
-        const float4 vb = __ldg(body_vel + b);
-        const float4 cm = __ldg(body_cm + b);
-        const float3 P = make_float3(p.x, p.y, p.z), V = make_float3(vb.x, vb.y, vb.z);
-        const float mind = S->rb_radius + S->fluid_radius + S->rb_eps;
-        float3 acc = make_float3(0.f, 0.f, 0.f);
-        const int rx = S->r2f_rel[0], ry = S->r2f_rel[1], rz = S->r2f_rel[2];
-        for (int z = -rz; z <= rz; z++) {
-            const uint32_t hz = fg_axis_hash_rel(p.z, S->cell[2], z, FG_PZ);
-            for (int y = -ry; y <= ry; y++) {
-                const uint32_t hy = fg_axis_hash_rel(p.y, S->cell[1], y, FG_PY);
-                for (int x = -rx; x <= rx; x++) {
-                    const uint32_t hx = fg_axis_hash_rel(p.x, S->cell[0], x, FG_PX);
-                    const uint32_t bk = S->bucket_base + fg_bucket(hx, hy, hz, S->nb, S->nb_mask);
-                    const uint32_t st = __ldg(fl_start + bk);
-                    if (st == FG_EMPTY) continue;
-                    const uint32_t en = __ldg(fl_end + bk);
-                    for (uint32_t j = st; j < en; j++)
-                        fg_contact(acc, P, V, __ldg(fl_spos + j), __ldg(fl_svel + j), mind, S->ck, S->ckd);
-                }
-            }
-        }
-        const float lw = (float)(b - (int)S->body_base); /* the reference stores the body index in w */
-        const float dx = p.x - cm.x, dy = p.y - cm.y, dz = p.z - cm.z;
-        float4 f = make_float4(acc.x, acc.y, acc.z, lw);
-        float4 t = make_float4(dy * acc.z - dz * acc.y, dz * acc.x - dx * acc.z, dx * acc.y - dy * acc.x, lw);
-        const uint32_t oi = rb_ids ? __ldg(rb_ids + i) : i;
-        if (add) {
-            float4 f0 = force[oi], t0 = torque[oi];
-            f.x += f0.x; f.y += f0.y; f.z += f0.z;
-            t.x += t0.x; t.y += t0.y; t.z += t0.z;
-        }
-        force[oi] = f;
-        torque[oi] = t;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t w = blockIdx.x >> 5;
+    if (w >= nwork) return;
+    const FgWork it = fg_work(work, w, n_single);
+    const uint32_t k = ((blockIdx.x & 31u) * RBF_WARPS) + (uint32_t)wid;
+    if (k >= it.count) return; /* warp-uniform */
+    const FgScene *S = fg_scene(table, &single, it.scene);
+    const uint32_t i = it.first + k;
+    const float4 p = rb_spos[i];
+    const int b = (int)p.w;
+    const float4 vb = __ldg(body_vel + b);
+    const float3 P = make_float3(p.x, p.y, p.z), V = make_float3(vb.x, vb.y, vb.z);
+    const float mind = S->rb_radius + S->fluid_radius + S->rb_eps;
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+    const int rx = S->r2f_rel[0], ry = S->r2f_rel[1], rz = S->r2f_rel[2];
+    const int nx = 2 * rx + 1, ny = 2 * ry + 1, nz = 2 * rz + 1;
+    for (int q = lane; q < nx * ny * nz; q += 32) {
+        const int z = q / (nx * ny) - rz, y = (q / nx) % ny - ry, x = q % nx - rx;
+        const uint32_t bk = S->bucket_base + fg_bucket(fg_axis_hash_rel(p.x, S->cell[0], x, FG_PX),
+                                                       fg_axis_hash_rel(p.y, S->cell[1], y, FG_PY),
+                                                       fg_axis_hash_rel(p.z, S->cell[2], z, FG_PZ), S->nb, S->nb_mask);
+        const uint32_t st = __ldg(fl_start + bk);
+        if (st == FG_EMPTY) continue;
+        const uint32_t en = __ldg(fl_end + bk);
+        for (uint32_t j = st; j < en; j++)
+            fg_contact(acc, P, V, __ldg(fl_spos + j), __ldg(fl_svel + j), mind, S->ck, S->ckd);
     }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+    }
+    if (lane) return;
+    const float4 cm = __ldg(body_cm + b);
+    const float lw = (float)(b - (int)S->body_base); /* the reference stores the body index in w */
+    const float dx = p.x - cm.x, dy = p.y - cm.y, dz = p.z - cm.z;
+    float4 f = make_float4(acc.x, acc.y, acc.z, lw);
+    float4 t = make_float4(dy * acc.z - dz * acc.y, dz * acc.x - dx * acc.z, dx * acc.y - dy * acc.x, lw);
+    const uint32_t oi = rb_ids ? __ldg(rb_ids + i) : i;
+    if (add) {
+        const float4 f0 = force[oi], t0 = torque[oi];
+        f.x += f0.x; f.y += f0.y; f.z += f0.z;
+        t.x += t0.x; t.y += t0.y; t.z += t0.z;
+    }
+    force[oi] = f;
+    torque[oi] = t;
 }
 
 void launch_rb_from_fluid(const Launch &L, const float4 *rb_spos, const uint32_t *rb_ids, const float4 *body_vel,
@@ -82,9 +94,10 @@ void launch_rb_from_fluid(const Launch &L, const float4 *rb_spos, const uint32_t
                           const uint32_t *fl_start, const uint32_t *fl_end, float4 *force, float4 *torque, int add)
 {
     if (!L.nwork) return;
-    k_rb_from_fluid<<<grid_for(L.nwork, 16), FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single,
-                                                                      rb_spos, rb_ids, body_vel, body_cm, fl_spos,
-                                                                      fl_svel, fl_start, fl_end, force, torque, add);
+    /* a work item holds up to FG_CHUNK spheres: FG_CHUNK / RBF_WARPS CTAs */
+    k_rb_from_fluid<<<L.nwork * (FG_CHUNK / RBF_WARPS), RBF_WARPS * 32, 0, L.stream>>>(
+        L.work, L.nwork, L.n, L.table, *L.single, rb_spos, rb_ids, body_vel, body_cm, fl_spos, fl_svel, fl_start,
+        fl_end, force, torque, add);
 }
 
 /* Sphere/sphere contact between different bodies of one scene (same rigid
@@ -210,6 +223,42 @@ __device__ __forceinline__ d4 qprod_d(d4 a, d4 b)
 
 #define BODY_THREADS 256
 
+/* FP64 partial force/torque sums of one body's spheres: chunk blockIdx.x of
+ * FG_BODY_CHUNKS, body blockIdx.y; threads stride the chunk, then a warp
+ * shuffle tree and the warps in order (deterministic). */
+__global__ void __launch_bounds__(BODY_THREADS) k_body_partial(const uint32_t *__restrict__ body_first,
+                                                              const uint32_t *__restrict__ body_count,
+                                                              const float4 *__restrict__ force,
+                                                              const float4 *__restrict__ torque,
+                                                              double *__restrict__ partial)
+{
+    __shared__ double s_red[BODY_THREADS / 32][8];
+    const uint32_t b = blockIdx.y, c = blockIdx.x;
+    const uint32_t first = body_first[b], cnt = body_count[b];
+    const uint32_t per = (cnt + FG_BODY_CHUNKS - 1) / FG_BODY_CHUNKS;
+    const uint32_t lo = min(cnt, c * per), hi = min(cnt, lo + per);
+    double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t k = lo + threadIdx.x; k < hi; k += BODY_THREADS) {
+        const float4 f = __ldg(force + first + k), t = __ldg(torque + first + k);
+        a[0] += f.x; a[1] += f.y; a[2] += f.z; a[3] += f.w;
+        a[4] += t.x; a[5] += t.y; a[6] += t.z; a[7] += t.w;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+#pragma unroll
+        for (int o = 16; o; o >>= 1) a[q] += __shfl_xor_sync(0xffffffffu, a[q], o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < 8; q++) s_red[wid][q] = a[q];
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        double v = 0.0;
+        for (int wv = 0; wv < BODY_THREADS / 32; wv++) v += s_red[wv][threadIdx.x];
+        partial[((size_t)b * FG_BODY_CHUNKS + c) * 8 + threadIdx.x] = v;
+    }
+}
+
 __global__ void __launch_bounds__(BODY_THREADS) k_body_update(const FgScene *__restrict__ table,
                                                              const __grid_constant__ FgScene single,
                                                              const uint32_t *__restrict__ body_scene,
@@ -221,7 +270,7 @@ __global__ void __launch_bounds__(BODY_THREADS) k_body_update(const FgScene *__r
 {
     __shared__ double s_red[BODY_THREADS / 32][8];
     for (uint32_t b = blockIdx.x; b < nbodies; b += gridDim.x) {
-        const uint32_t first = body_first[b], cnt = body_count[b];
+        const uint32_t first = body_first[b], cnt = st.partial ? 0u : body_count[b];
         double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (uint32_t k = threadIdx.x; k < cnt; k += BODY_THREADS) {
             float4 f = __ldg(force + first + k), t = __ldg(torque + first + k);
@@ -239,11 +288,20 @@ __global__ void __launch_bounds__(BODY_THREADS) k_body_update(const FgScene *__r
         __syncthreads();
         if (threadIdx.x == 0) {
             double F[4] = {0, 0, 0, 0}, T[4] = {0, 0, 0, 0};
-            for (int wv = 0; wv < BODY_THREADS / 32; wv++)
-                for (int c = 0; c < 4; c++) {
-                    F[c] += s_red[wv][c];
-                    T[c] += s_red[wv][4 + c];
-                }
+            if (st.partial) {
+                const double *pp = st.partial + (size_t)b * FG_BODY_CHUNKS * 8;
+                for (int ch = 0; ch < FG_BODY_CHUNKS; ch++)
+                    for (int c = 0; c < 4; c++) {
+                        F[c] += pp[ch * 8 + c];
+                        T[c] += pp[ch * 8 + 4 + c];
+                    }
+            } else {
+                for (int wv = 0; wv < BODY_THREADS / 32; wv++)
+                    for (int c = 0; c < 4; c++) {
+                        F[c] += s_red[wv][c];
+                        T[c] += s_red[wv][4 + c];
+                    }
+            }
             st.force_sum[b] = fg_d4(F[0], F[1], F[2], F[3]);
             st.torque_sum[b] = fg_d4(T[0], T[1], T[2], T[3]);
             /* mass 0: a static body (the reference's "static" rigid-body
@@ -324,6 +382,11 @@ void launch_body_update(const FgScene *table, const FgScene *single, const uint3
                         const float4 *force, const float4 *torque, BodyState st, int integrate, cudaStream_t s)
 {
     if (!nbodies) return;
+    if (st.partial && nbodies <= 65535u)
+        k_body_partial<<<dim3(FG_BODY_CHUNKS, nbodies), BODY_THREADS, 0, s>>>(body_first, body_count, force, torque,
+                                                                            st.partial);
+    else
+        st.partial = nullptr;
     k_body_update<<<grid_for(nbodies, 4), BODY_THREADS, 0, s>>>(table, *single, body_scene, body_first, body_count,
                                                                 nbodies, force, torque, st, integrate);
 }

@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                             if ((uint32_t)e < m) {
                                 const float dx = fmaf(-a[e].x, scale, px), dy = fmaf(-a[e].y, scale, py),
                                             dz = fmaf(-a[e].z, scale, pz);
-                                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                                const float r2 = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
                                 fg_pair(fx, fy, fz, dx, dy, dz, r2, h, kspiky, kv, rho_i, P_i, v, a[e].w, b[e].w,
                                         b[e]);
                             }
@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                         const float4 q0 = __ldg(list.rec + 2 * j);
                         const float dx = fmaf(-q0.x, scale, px), dy = fmaf(-q0.y, scale, py),
                                     dz = fmaf(-q0.z, scale, pz);
-                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
                         if (r2 <= h2) {
                             const float4 q1 = __ldg(list.rec + 2 * j + 1);
                             fg_pair(fx, fy, fz, dx, dy, dz, r2, h, kspiky, kv, rho_i, P_i, v, q0.w, q1.w, q1);
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                     if (j == i) return;
                     const float4 q = __ldg(spos + j);
                     const float dx = fmaf(-q.x, scale, px), dy = fmaf(-q.y, scale, py), dz = fmaf(-q.z, scale, pz);
-                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
                     if (r2 <= h2) {
                         const float4 vj = __ldg(svel + j);
                         const float2 dj = __ldg(dp + j);

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(CC_WARPS * 32) k_density_cc(const FgScene *__r
                             const float4 q = cand[c];
                             const float dx = fmaf(-q.x, scale, tx), dy = fmaf(-q.y, scale, ty),
                                         dz = fmaf(-q.z, scale, tz);
-                            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                            const float r2 = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
                             if (r2 < h2) {
                                 const float tt = h2 - r2;
                                 const float y = tt * tt * tt - kc;
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(CC_WARPS * 32) k_forces_cc(const FgScene *__re
                                 const float4 q = c0s[c];
                                 const float dx = fmaf(-q.x, scale, tx), dy = fmaf(-q.y, scale, ty),
                                             dz = fmaf(-q.z, scale, tz);
-                                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                                const float r2 = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
                                 in = (r2 <= h2) && (cjs[c] != tj);
                             }
                             const uint32_t m = __ballot_sync(0xffffffffu, in);
@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(CC_WARPS * 32) k_forces_cc(const FgScene *__re
                             const float4 q0 = c0s[c], q1 = c1s[c];
                             const float dx = fmaf(-q0.x, scale, tx), dy = fmaf(-q0.y, scale, ty),
                                         dz = fmaf(-q0.z, scale, tz);
-                            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                            const float r2 = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
                             fg_pair(px, py, pz, dx, dy, dz, r2, h, kspiky, kv, trho, tprs, tv, q0.w, q1.w, q1);
                         }
                         px = cc_sum(px);

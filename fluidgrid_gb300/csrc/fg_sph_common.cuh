@@ -229,17 +229,19 @@ __device__ __forceinline__ void fg_pair(float &fx, float &fy, float &fz, float d
                                         float h, float kspiky, float kv, float rho_i, float P_i, float4 vi,
                                         float rho_j, float P_j, float4 vj)
 {
+    /* every operation rounded on its own: the same bits in every kernel */
     const float il = rsqrtf(r2);
-    const float l = r2 * il;
-    const float hl = h - l;
-    const float irr = __fdividef(1.0f, rho_i * rho_j); /* rho >= 1: no denormal or overflow range */
+    const float l = __fmul_rn(r2, il);
+    const float hl = __fsub_rn(h, l);
+    const float irr = __fdividef(1.0f, __fmul_rn(rho_i, rho_j)); /* rho >= 1: no denormal or overflow range */
     /* pressure: -(d/l) kSpiky (h-l)^2 (Pi+Pj)/(rho_i rho_j) */
-    const float cp = -(kspiky * hl * hl) * ((P_i + P_j) * irr) * il;
+    const float cp = __fmul_rn(__fmul_rn(-__fmul_rn(__fmul_rn(kspiky, hl), hl), __fmul_rn(__fadd_rn(P_i, P_j), irr)),
+                               il);
     /* viscosity: (vj-vi)/(rho_i rho_j) kVisc (h-l) mu */
-    const float cv = (kv * hl) * irr;
-    fx += dx * cp + (vj.x - vi.x) * cv;
-    fy += dy * cp + (vj.y - vi.y) * cv;
-    fz += dz * cp + (vj.z - vi.z) * cv;
+    const float cv = __fmul_rn(__fmul_rn(kv, hl), irr);
+    fx = __fadd_rn(fx, __fmaf_rn(__fsub_rn(vj.x, vi.x), cv, __fmul_rn(dx, cp)));
+    fy = __fadd_rn(fy, __fmaf_rn(__fsub_rn(vj.y, vi.y), cv, __fmul_rn(dy, cp)));
+    fz = __fadd_rn(fz, __fmaf_rn(__fsub_rn(vj.z, vi.z), cv, __fmul_rn(dz, cp)));
 }
 
 /* Tail of SPHCalculateForcesK / SPHCalculateForcesWithSRBK
