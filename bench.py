@@ -379,8 +379,8 @@ def run_ours(args, rank, world, local):
         forms["batched"] = run_batched()
     if "served" in args.forms:
         forms["served"] = run_served(duration=args.served_seconds)
-        # latency-bounded serving: at most 1M particles advanced per step
-        forms["served_latency"] = run_served(duration=args.served_seconds / 2, max_particles=1_000_000,
+        # latency-bounded serving: at most 750k particles advanced per step
+        forms["served_latency"] = run_served(duration=args.served_seconds / 2, max_particles=750_000,
                                              label="served_latency_bounded")
     if rank == 0:
         peak, peak_kind = measured_peaks()

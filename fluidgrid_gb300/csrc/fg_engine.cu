@@ -86,6 +86,10 @@ World::~World()
         if (g.graph) cudaGraphDestroy(g.graph);
     }
     for (void *p : allocs) cudaFree(p);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_fluid_ready) cudaEventDestroy(ev_fluid_ready);
+    if (ev_rb_done) cudaEventDestroy(ev_rb_done);
+    if (stream2) cudaStreamDestroy(stream2);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -370,6 +374,9 @@ int World::set_layout(const fg_scene_desc *d, uint32_t ns)
         if (d[s].n_bodies && d[s].rb_rb_contact) any_rb_rb = true;
     }
     n = (uint32_t)np;
+    rb_small_scenes = true;
+    for (uint32_t s = 0; s < ns; s++)
+        if (scenes_h[s].nsph > FG_RB_SCENE_MAX) rb_small_scenes = false;
     total_buckets = (uint32_t)nbk;
     nspheres = (uint32_t)nsph;
     nbodies = (uint32_t)nbod;
@@ -493,6 +500,10 @@ int World::init_stream(cudaStream_t st)
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         own_stream = true;
     }
+    CK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_fluid_ready, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_rb_done, cudaEventDisableTiming));
     return FG_OK;
 }
 
@@ -553,6 +564,52 @@ __global__ void k_aabb_reset(int *aabb, uint32_t ns)
     if (i < 6 * ns) aabb[i] = (i % 6) < 3 ? fg_float_ord(3.0e38f) : fg_float_ord(-3.0e38f);
 }
 
+/* Rigid-sphere grid of every scene: AABB, world positions and keys, sort,
+ * start/end (the stage bit FG_STAGE_RB_GRID). */
+void World::enqueue_rb_grid(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches)
+{
+    if (!(stages & FG_STAGE_RB_GRID)) return;
+    if (ev) cudaEventRecord(ev[8], st);
+    Launch Ls = sphere_launch();
+    Ls.stream = st;
+    k_aabb_reset<<<(6 * nscenes + 127) / 128, 128, 0, st>>>(aabb, nscenes);
+    launch_hash_with_offset(Ls, rb_local, bxf, bqf, rb_world, rb_keys_u, nullptr, aabb);
+    if (rb_small_scenes) {
+        launch_rb_sort_ranges(single ? nullptr : scenes_d, &scenes_h[0], nscenes, rb_keys_u, rb_world, rb_keys,
+                              rb_ids, rb_spos, rb_start, rb_end, st);
+        launches += 3;
+    } else {
+        radix_sort(rb_keys_u, nullptr, rb_keys, rb_ids, nspheres, rb_key_bits, 8, rs, st);
+        cudaMemsetAsync(rb_start, 0xff, 4 * (size_t)total_rb_buckets, st);
+        launch_cell_ranges(rb_keys, rb_ids, rb_world, nullptr, rb_start, rb_end, rb_spos, nullptr, nspheres, st);
+        launches += 3 + 3 * radix_passes(rb_key_bits, 8);
+    }
+    if (ev) cudaEventRecord(ev[9], st);
+}
+
+/* Sphere forces and torques from the fluid (and from other bodies) (the
+ * stage bit FG_STAGE_RB_CONTACT). */
+void World::enqueue_rb_contact(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches)
+{
+    if (!(stages & FG_STAGE_RB_CONTACT)) return;
+    if (ev) cudaEventRecord(ev[10], st);
+    Launch Ls = sphere_launch();
+    Ls.stream = st;
+    launch_rb_from_fluid(Ls, rb_spos, rb_ids, bvf, bxf, spos, svel, start, end, rb_force, rb_torque, 0);
+    launches++;
+    if (any_rb_rb) {
+        launch_rb_from_rb(Ls, rb_spos, rb_ids, bvf, bxf, rb_start, rb_end, rb_force, rb_torque, nullptr, 1);
+        launches++;
+    }
+    if (ev) cudaEventRecord(ev[11], st);
+}
+
+#define CK0(call)                                                                                  \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) set_error(#call, e_);                                               \
+    } while (0)
+
 uint32_t World::enqueue_step(cudaEvent_t *ev)
 {
     /* ev: optional 16 events, (2k, 2k+1) bracket stage bit k */
@@ -561,6 +618,18 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
     };
     uint32_t launches = 0;
     const Launch L = fluid_launch();
+    const bool rb = nbodies > 0;
+    /* the rigid-sphere grid needs only the previous step's body poses and the
+     * fluid/sphere contact only the fluid grid: in a full step they run on a
+     * second stream beside the fluid sort and density pass and join before
+     * the force pass (parallel branches of the captured graph) */
+    const uint32_t full = FG_STAGE_HASH | FG_STAGE_SORT | FG_STAGE_RANGES | FG_STAGE_RB_GRID | FG_STAGE_RB_CONTACT;
+    const bool fork = rb && !ev && rb_small_scenes && stream2 && (stages & full) == full;
+    if (fork) {
+        CK0(cudaEventRecord(ev_fork, stream));
+        CK0(cudaStreamWaitEvent(stream2, ev_fork, 0));
+        enqueue_rb_grid(stream2, nullptr, launches);
+    }
     if (stages & FG_STAGE_HASH) {
         mark(0, 0);
         launch_hash(L, pos, keys_u, nullptr);
@@ -585,6 +654,12 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         mark(2, 1);
         launches += 1;
     }
+    if (fork) {
+        CK0(cudaEventRecord(ev_fluid_ready, stream));
+        CK0(cudaStreamWaitEvent(stream2, ev_fluid_ready, 0));
+        enqueue_rb_contact(stream2, nullptr, launches);
+        CK0(cudaEventRecord(ev_rb_done, stream2));
+    }
     if (stages & FG_STAGE_DENSITY) {
         mark(3, 0);
         if (use_cc)
@@ -596,28 +671,11 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         mark(3, 1);
         launches++;
     }
-    const bool rb = nbodies > 0;
-    const Launch Ls = sphere_launch();
-    if (rb && (stages & FG_STAGE_RB_GRID)) {
-        mark(4, 0);
-        k_aabb_reset<<<(6 * nscenes + 127) / 128, 128, 0, stream>>>(aabb, nscenes);
-        launch_hash_with_offset(Ls, rb_local, bxf, bqf, rb_world, rb_keys_u, nullptr, aabb);
-        radix_sort(rb_keys_u, nullptr, rb_keys, rb_ids, nspheres, rb_key_bits, 8, rs, stream);
-        cudaMemsetAsync(rb_start, 0xff, 4 * (size_t)total_rb_buckets, stream);
-        launch_cell_ranges(rb_keys, rb_ids, rb_world, nullptr, rb_start, rb_end, rb_spos, nullptr, nspheres, stream);
-        mark(4, 1);
-        launches += 3 + 3 * radix_passes(rb_key_bits, 8);
+    if (rb && !fork) {
+        enqueue_rb_grid(stream, ev, launches);
+        enqueue_rb_contact(stream, ev, launches);
     }
-    if (rb && (stages & FG_STAGE_RB_CONTACT)) {
-        mark(5, 0);
-        launch_rb_from_fluid(Ls, rb_spos, rb_ids, bvf, bxf, spos, svel, start, end, rb_force, rb_torque, 0);
-        launches++;
-        if (any_rb_rb) {
-            launch_rb_from_rb(Ls, rb_spos, rb_ids, bvf, bxf, rb_start, rb_end, rb_force, rb_torque, nullptr, 1);
-            launches++;
-        }
-        mark(5, 1);
-    }
+    if (fork) CK0(cudaStreamWaitEvent(stream, ev_rb_done, 0));
     if (stages & FG_STAGE_FORCES) {
         mark(6, 0);
         RigidGrid G;
@@ -888,7 +946,8 @@ uint32_t World::launches_per_step()
     if (stages & FG_STAGE_RANGES) c += 1; /* + one memset node */
     if (stages & FG_STAGE_DENSITY) c += 1;
     if (nbodies) {
-        if (stages & FG_STAGE_RB_GRID) c += 3 + 3 * radix_passes(rb_key_bits, 8); /* aabb reset, hash, ranges */
+        if (stages & FG_STAGE_RB_GRID) /* aabb reset, hash, sort + ranges */
+            c += rb_small_scenes ? 3 : 3 + 3 * radix_passes(rb_key_bits, 8);
         if (stages & FG_STAGE_RB_CONTACT) c += 1 + (any_rb_rb ? 1 : 0);
         if (stages & FG_STAGE_BODIES) c += 1;
     }

@@ -36,6 +36,7 @@ struct World {
     uint32_t key_bits = 0, rb_key_bits = 0, digit_bits = 8;
     bool single = true;
     bool any_rb_rb = false;
+    bool rb_small_scenes = true; /* every scene has <= FG_RB_SCENE_MAX spheres: one-CTA rigid grid */
     std::vector<FgScene> scenes_h;
     FgScene *scenes_d = nullptr;
     FgWork *work_d = nullptr, *work_sph_d = nullptr;
@@ -77,6 +78,10 @@ struct World {
     /* execution */
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    cudaStream_t stream2 = nullptr; /* rigid-body branch of a full step */
+    cudaEvent_t ev_fork = nullptr, ev_fluid_ready = nullptr, ev_rb_done = nullptr;
+    void enqueue_rb_grid(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches);
+    void enqueue_rb_contact(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches);
     uint32_t stages = 255;
     bool fused_integrate = true;
     bool use_graphs = true;

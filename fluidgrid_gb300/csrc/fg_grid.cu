@@ -454,6 +454,71 @@ void launch_morton_keys(const Launch &L, const float4 *pos, uint32_t *keys, uint
                                                                     keys, bits, scene_shift);
 }
 
+/* ------------------------------------------ rigid-sphere grid per scene
+ * The sort + start/end of FindCellOffsetOrderingPosK (K_HashGrid.cu:140-197)
+ * for the rigid-sphere grid, in one CTA per scene when every scene has at
+ * most FG_RB_SCENE_MAX spheres.  The scene's (key, index) pairs are sorted
+ * as 64-bit words by a bitonic network in shared memory -- the index in the
+ * low word makes the order the stable one, so keys, ids and ranges equal the
+ * radix path's bit for bit.  A scene's spheres and rigid buckets are its own
+ * ranges of the global arrays, and the global stable order is the scenes'
+ * orders one after another (keys carry the scene's rigid bucket base). */
+__global__ void __launch_bounds__(1024) k_rb_sort_ranges(const FgScene *__restrict__ table,
+                                                        const __grid_constant__ FgScene single,
+                                                        const uint32_t *__restrict__ keys_u,
+                                                        const float4 *__restrict__ world,
+                                                        uint32_t *__restrict__ keys, uint32_t *__restrict__ ids,
+                                                        float4 *__restrict__ spos, uint32_t *__restrict__ rstart,
+                                                        uint32_t *__restrict__ rend)
+{
+    __shared__ unsigned long long s[FG_RB_SCENE_MAX];
+    const FgScene *S = table ? table + blockIdx.x : &single;
+    const uint32_t n = S->nsph, base = S->sph_base;
+    if (!(S->flags & FG_SCENE_HAS_RB)) return; /* the scene has no rigid buckets */
+    for (uint32_t b = threadIdx.x; b < S->rb_nb; b += blockDim.x) rstart[S->rb_bucket_base + b] = FG_EMPTY;
+    if (!n) return;
+    uint32_t P = 1;
+    while (P < n) P <<= 1;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
+        s[i] = i < n ? (((unsigned long long)__ldg(keys_u + base + i) << 32) | i) : ~0ull;
+    __syncthreads();
+    for (uint32_t k = 2; k <= P; k <<= 1)
+        for (uint32_t j = k >> 1; j; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+                const uint32_t l = i ^ j;
+                if (l > i) {
+                    const unsigned long long a = s[i], c = s[l];
+                    if ((a > c) == ((i & k) == 0)) {
+                        s[i] = c;
+                        s[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const unsigned long long v = s[i];
+        const uint32_t key = (uint32_t)(v >> 32), id = base + (uint32_t)(v & 0xffffffffu);
+        keys[base + i] = key;
+        ids[base + i] = id;
+        spos[base + i] = __ldg(world + id);
+        const uint32_t prev = i ? (uint32_t)(s[i - 1] >> 32) : key;
+        if (i == 0 || key != prev) {
+            rstart[key] = base + i;
+            if (i) rend[prev] = base + i;
+        }
+        if (i == n - 1) rend[key] = base + n;
+    }
+}
+
+void launch_rb_sort_ranges(const FgScene *table, const FgScene *single, uint32_t nscenes, const uint32_t *keys_u,
+                           const float4 *world, uint32_t *keys, uint32_t *ids, float4 *spos, uint32_t *rstart,
+                           uint32_t *rend, cudaStream_t s)
+{
+    if (!nscenes) return;
+    k_rb_sort_ranges<<<nscenes, 1024, 0, s>>>(table, *single, keys_u, world, keys, ids, spos, rstart, rend);
+}
+
 __global__ void k_fill(uint32_t *buf, size_t words, uint32_t v)
 {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x)

@@ -50,6 +50,14 @@ void launch_cell_ranges(const uint32_t *keys, const uint32_t *ids, const float4 
                         uint32_t *start, uint32_t *end, float4 *spos, float4 *svel, uint32_t n, cudaStream_t st,
                         uint32_t *inv = nullptr, uint32_t *runs = nullptr, uint32_t *nruns = nullptr);
 
+/* Rigid-sphere grid of every scene (sort by key, ids, sorted positions,
+ * start/end) in one CTA per scene; valid when no scene has more than
+ * FG_RB_SCENE_MAX spheres.  keys_u are global rigid bucket ids. */
+#define FG_RB_SCENE_MAX 4096u
+void launch_rb_sort_ranges(const FgScene *table, const FgScene *single, uint32_t nscenes, const uint32_t *keys_u,
+                           const float4 *world, uint32_t *keys, uint32_t *ids, float4 *spos, uint32_t *rstart,
+                           uint32_t *rend, cudaStream_t s);
+
 /* Spatial (Morton) keys of the unsorted particles: scene id << scene_shift |
  * Morton code of the cell with `bits` bits per axis (bits <= 10). */
 void launch_morton_keys(const Launch &L, const float4 *pos, uint32_t *keys, uint32_t bits, uint32_t scene_shift);
