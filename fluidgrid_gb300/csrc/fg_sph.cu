@@ -169,8 +169,11 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                     /* in-range neighbours without self, four indices per
                      * 16-byte load, then all eight record loads in flight */
                     const uint32_t *nl = list.idx + (size_t)tpos * list.cap;
+                    uint4 qn = c ? __ldg(reinterpret_cast<const uint4 *>(nl)) : make_uint4(0u, 0u, 0u, 0u);
                     for (uint32_t k = 0; k < c; k += 4) {
-                        const uint4 q = __ldg(reinterpret_cast<const uint4 *>(nl + k));
+                        /* the next four indices load while these records do */
+                        const uint4 q = qn;
+                        if (k + 4u < c) qn = __ldg(reinterpret_cast<const uint4 *>(nl + k + 4u));
                         const uint32_t jj[4] = {q.x, q.y, q.z, q.w};
                         const uint32_t m = min(4u, c - k);
                         float4 a[4], b[4];
