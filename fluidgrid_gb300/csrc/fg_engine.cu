@@ -89,6 +89,7 @@ World::~World()
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_fluid_ready) cudaEventDestroy(ev_fluid_ready);
     if (ev_rb_done) cudaEventDestroy(ev_rb_done);
+    if (ev_bodies_done) cudaEventDestroy(ev_bodies_done);
     if (stream2) cudaStreamDestroy(stream2);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
@@ -321,6 +322,7 @@ int World::reserve(const Capacity &c)
         if ((r = A((void **)&bts, 32 * B))) return r;
         if ((r = A((void **)&bxf, 16 * B))) return r;
         if ((r = A((void **)&bvf, 16 * B))) return r;
+        if ((r = A((void **)&bvf_next, 16 * B))) return r;
         if ((r = A((void **)&bqf, 16 * B))) return r;
         if ((r = A((void **)&bmass, 8 * B))) return r;
         if ((r = A((void **)&binv, 72 * B))) return r;
@@ -504,6 +506,7 @@ int World::init_stream(cudaStream_t st)
     CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_fluid_ready, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_rb_done, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_bodies_done, cudaEventDisableTiming));
     return FG_OK;
 }
 
@@ -610,6 +613,21 @@ void World::enqueue_rb_contact(cudaStream_t st, cudaEvent_t *ev, uint32_t &launc
         if (e_ != cudaSuccess) set_error(#call, e_);                                               \
     } while (0)
 
+/* Per-body FP64 force/torque sums and the integration (the stage bit
+ * FG_STAGE_BODIES); the FP32 velocity mirror goes to vf. */
+void World::enqueue_bodies(cudaStream_t st, float4 *vf)
+{
+    BodyState b;
+    b.x = bx; b.v = bv; b.q = bq; b.L = bL;
+    b.inv_inertia = binv;
+    b.mass = bmass;
+    b.x_f = bxf; b.v_f = vf; b.q_f = bqf;
+    b.force_sum = bfs; b.torque_sum = bts;
+    b.partial = body_part;
+    launch_body_update(single ? nullptr : scenes_d, &scenes_h[0], body_scene, body_first, body_count, nbodies,
+                       rb_force, rb_torque, b, 1, st);
+}
+
 uint32_t World::enqueue_step(cudaEvent_t *ev)
 {
     /* ev: optional 16 events, (2k, 2k+1) bracket stage bit k */
@@ -654,11 +672,22 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         mark(2, 1);
         launches += 1;
     }
+    /* with a full step forked, the body reduction and integration follow the
+     * contact on the second stream and overlap the force pass, which reads
+     * only the spheres' grid and the bodies' old velocities (kept in bvf
+     * until the step's end) */
+    const bool fork_bodies = fork && (stages & (FG_STAGE_FORCES | FG_STAGE_BODIES)) ==
+                                         (FG_STAGE_FORCES | FG_STAGE_BODIES);
     if (fork) {
         CK0(cudaEventRecord(ev_fluid_ready, stream));
         CK0(cudaStreamWaitEvent(stream2, ev_fluid_ready, 0));
         enqueue_rb_contact(stream2, nullptr, launches);
         CK0(cudaEventRecord(ev_rb_done, stream2));
+        if (fork_bodies) {
+            enqueue_bodies(stream2, bvf_next);
+            launches += body_launches();
+            CK0(cudaEventRecord(ev_bodies_done, stream2));
+        }
     }
     if (stages & FG_STAGE_DENSITY) {
         mark(3, 0);
@@ -703,19 +732,16 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         }
         mark(6, 1);
     }
-    if (rb && (stages & FG_STAGE_BODIES)) {
+    if (fork_bodies) {
+        /* the body update ran beside the force pass; its velocity mirror
+         * lands once the force pass has read the old one */
+        CK0(cudaStreamWaitEvent(stream, ev_bodies_done, 0));
+        CK0(cudaMemcpyAsync(bvf, bvf_next, 16 * (size_t)nbodies, cudaMemcpyDeviceToDevice, stream));
+    } else if (rb && (stages & FG_STAGE_BODIES)) {
         mark(7, 0);
-        BodyState b;
-        b.x = bx; b.v = bv; b.q = bq; b.L = bL;
-        b.inv_inertia = binv;
-        b.mass = bmass;
-        b.x_f = bxf; b.v_f = bvf; b.q_f = bqf;
-        b.force_sum = bfs; b.torque_sum = bts;
-        b.partial = body_part;
-        launch_body_update(single ? nullptr : scenes_d, &scenes_h[0], body_scene, body_first, body_count, nbodies,
-                           rb_force, rb_torque, b, 1, stream);
+        enqueue_bodies(stream, bvf);
         mark(7, 1);
-        launches++;
+        launches += body_launches();
     }
     return launches;
 }
@@ -949,7 +975,7 @@ uint32_t World::launches_per_step()
         if (stages & FG_STAGE_RB_GRID) /* aabb reset, hash, sort + ranges */
             c += rb_small_scenes ? 3 : 3 + 3 * radix_passes(rb_key_bits, 8);
         if (stages & FG_STAGE_RB_CONTACT) c += 1 + (any_rb_rb ? 1 : 0);
-        if (stages & FG_STAGE_BODIES) c += 1;
+        if (stages & FG_STAGE_BODIES) c += body_launches();
     }
     if (stages & FG_STAGE_FORCES) c += fused_integrate ? 1 : 2;
     return c;

@@ -70,6 +70,7 @@ struct World {
     FgD4 *bx = nullptr, *bv = nullptr, *bq = nullptr, *bL = nullptr, *bfs = nullptr, *bts = nullptr;
     double *body_part = nullptr; /* FG_BODY_CHUNKS x 8 FP64 partial sums per body */
     float4 *bxf = nullptr, *bvf = nullptr, *bqf = nullptr;
+    float4 *bvf_next = nullptr; /* velocity mirror written beside the force pass */
     double *bmass = nullptr, *binv = nullptr;
     uint32_t *body_scene = nullptr, *body_first = nullptr, *body_count = nullptr;
     uint32_t *status_d = nullptr;
@@ -79,9 +80,13 @@ struct World {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaStream_t stream2 = nullptr; /* rigid-body branch of a full step */
-    cudaEvent_t ev_fork = nullptr, ev_fluid_ready = nullptr, ev_rb_done = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_fluid_ready = nullptr, ev_rb_done = nullptr, ev_bodies_done = nullptr;
     void enqueue_rb_grid(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches);
     void enqueue_rb_contact(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches);
+    void enqueue_bodies(cudaStream_t st, float4 *vf);
+    /* kernels of one body update: the chunked FP64 partial sums (up to 65,535
+     * bodies) and the update */
+    uint32_t body_launches() const { return nbodies <= 65535u ? 2u : 1u; }
     uint32_t stages = 255;
     bool fused_integrate = true;
     bool use_graphs = true;
