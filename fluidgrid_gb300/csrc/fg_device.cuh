@@ -66,6 +66,15 @@ __device__ __forceinline__ uint32_t fg_axis_hash_rel(float p, float cell, int o,
     return (uint32_t)fg_axis_index(__fadd_rn(p, off), cell) * prime;
 }
 
+/* One 32-byte neighbour record (two float4) in a single 256-bit load of
+ * read-only data; p must be 32-byte aligned. */
+__device__ __forceinline__ void fg_ld_rec(const float4 *p, float4 &a, float4 &b)
+{
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
 /* select one of three register values without local-memory indexing */
 __device__ __forceinline__ uint32_t fg_sel3(uint32_t a0, uint32_t a1, uint32_t a2, int k)
 {

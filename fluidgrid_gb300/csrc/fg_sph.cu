@@ -167,7 +167,8 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                 const uint32_t c = list.cnt[tpos];
                 if (c <= list.cap) {
                     /* in-range neighbours without self, four indices per
-                     * 16-byte load, then all eight record loads in flight */
+                     * 16-byte load, then the four 32-byte records in
+                     * flight, one 256-bit load each */
                     const uint32_t *nl = list.idx + (size_t)tpos * list.cap;
                     uint4 qn = c ? __ldg(reinterpret_cast<const uint4 *>(nl)) : make_uint4(0u, 0u, 0u, 0u);
                     for (uint32_t k = 0; k < c; k += 4) {
@@ -180,8 +181,7 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
 #pragma unroll
                         for (int e = 0; e < 4; e++) {
                             const uint32_t j = (uint32_t)e < m ? jj[e] : jj[0];
-                            a[e] = __ldg(list.rec + 2 * j);
-                            b[e] = __ldg(list.rec + 2 * j + 1);
+                            fg_ld_rec(list.rec + 2 * j, a[e], b[e]);
                         }
 #pragma unroll
                         for (int e = 0; e < 4; e++) {
