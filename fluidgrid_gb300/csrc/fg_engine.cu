@@ -849,6 +849,7 @@ void World::tune_begin()
                 tr.ncand = 0;
                 return;
             }
+    tr.prev = tr.dim == 0 ? current_kernel() : (tr.dim == 1 ? (int)ctas_per_sm : (int)digit_bits);
     tr.idx = 0;
     tr.active = true;
 }
@@ -865,16 +866,20 @@ int World::tune_finish()
     tr.active = false;
     CK(cudaEventSynchronize(tr.ev[2 * tr.ncand - 1]));
     int best = tr.cand[0];
-    float best_ms = 1e30f;
+    float best_ms = 1e30f, cur_ms = -1.0f;
     for (int c = 0; c < tr.ncand; c++) {
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, tr.ev[2 * c], tr.ev[2 * c + 1]));
         if (tr.dim == 0) tune_last_ms[tr.cand[c]] = ms;
+        if (tr.cand[c] == tr.prev) cur_ms = ms;
         if (ms < best_ms) {
             best_ms = ms;
             best = tr.cand[c];
         }
     }
+    /* one step per candidate is a noisy sample: the value in use stays
+     * unless another is faster by more than 1.5% */
+    if (cur_ms >= 0.0f && best != tr.prev && best_ms > cur_ms * (1.0f - FG_TUNE_MARGIN)) best = tr.prev;
     tune_apply(tr.dim, best);
     return FG_OK;
 }
@@ -931,19 +936,19 @@ int World::step(uint32_t nsteps)
         const bool refresh = use_order && !needs_runs() && (stages & FG_STAGE_DENSITY) &&
                              (!order_valid || (order_period && step_count % order_period == 0));
         if (refresh) enqueue_order_refresh();
-        if (tr.active) {
-            tune_apply(tr.dim, tr.cand[tr.idx]);
-            CK(cudaEventRecord(tr.ev[2 * tr.idx], stream));
-        }
+        if (tr.active) tune_apply(tr.dim, tr.cand[tr.idx]);
         const int kused = current_kernel();
-        if (!use_graphs) {
-            enqueue_step();
-        } else {
-            cudaGraphExec_t ge = nullptr;
+        /* the graph is found (or captured and instantiated) before a trial's
+         * start event, so a candidate's first use is not charged the host
+         * time of building its graph */
+        cudaGraphExec_t ge = nullptr;
+        if (use_graphs) {
             int r = graph_for_current(&ge);
             if (r != FG_OK) return r;
-            CK(cudaGraphLaunch(ge, stream));
         }
+        if (tr.active) CK(cudaEventRecord(tr.ev[2 * tr.idx], stream));
+        if (!use_graphs) enqueue_step();
+        else CK(cudaGraphLaunch(ge, stream));
         if (tr.active) {
             CK(cudaEventRecord(tr.ev[2 * tr.idx + 1], stream));
             if (++tr.idx == tr.ncand) {

@@ -121,9 +121,11 @@ struct World {
         use_list = (k == 1);
     }
     bool needs_runs() const { return use_cc; }
+#define FG_TUNE_MARGIN 0.015f
     struct TuneRound {
         bool active = false;
         int dim = 0, ncand = 0, idx = 0;
+        int prev = 0; /* the tunable's value before the round */
         int cand[4] = {0, 0, 0, 0};
         cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     } tr;

@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(FG_CHUNK, 8) k_density(const FgWork *__restric
             const float px = p.x * scale, py = p.y * scale, pz = p.z * scale;
             const uint32_t cap = LIST ? list.cap : 0u;
             fg_walk27(p.x, p.y, p.z, S, start, end, [&](uint32_t j) {
-                acc.visit<LIST>(__ldg(spos + j), j, px, py, pz, scale, h2, i, lp, cap);
+                acc.visit<LIST>(__ldg(spos + j), j, px, py, pz, scale, h2, lp, cap);
             });
             if (LIST) acc.flush(lp, cap);
             const float mass = use_o ? mass_o : S->mass;
@@ -166,9 +166,10 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                 const float rho_i = r0.w, P_i = r1.w;
                 const uint32_t c = list.cnt[tpos];
                 if (c <= list.cap) {
-                    /* in-range neighbours without self, four indices per
-                     * 16-byte load, then the four 32-byte records in
-                     * flight, one 256-bit load each */
+                    /* in-range visits in walk order (the target's own
+                     * entries skipped), four indices per 16-byte load, then
+                     * the four 32-byte records in flight, one 256-bit load
+                     * each */
                     const uint32_t *nl = list.idx + (size_t)tpos * list.cap;
                     uint4 qn = c ? __ldg(reinterpret_cast<const uint4 *>(nl)) : make_uint4(0u, 0u, 0u, 0u);
                     for (uint32_t k = 0; k < c; k += 4) {
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                         }
 #pragma unroll
                         for (int e = 0; e < 4; e++) {
-                            if ((uint32_t)e < m) {
+                            if ((uint32_t)e < m && jj[e] != i) {
                                 const float dx = fmaf(-a[e].x, scale, px), dy = fmaf(-a[e].y, scale, py),
                                             dz = fmaf(-a[e].z, scale, pz);
                                 const float r2 = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));

@@ -46,10 +46,12 @@ __device__ __forceinline__ void fg_walk27(float px, float py, float pz, const Fg
 
 /* One target's state in a density pass: the Kahan sum of (h^2 - l^2)^3 over
  * the candidates with l <= h (an exact 0 at l = h, so the sum equals the
- * reference's l < h sum) and the force pass's neighbour list (l <= h, not
- * the target itself), buffered in registers and stored four entries at a
- * time.  Every operation is rounded on its own, so any kernel that visits the
- * same candidates in the same order produces the same bits. */
+ * reference's l < h sum) and the force pass's neighbour list (every visit
+ * with l <= h, the target's own entries included: testing j != i in the
+ * force pass, which waits on memory, is cheaper than in this issue-bound
+ * branch), buffered in registers and stored four entries at a time.  Every
+ * operation is rounded on its own, so any kernel that visits the same
+ * candidates in the same order produces the same bits. */
 struct DensityAcc {
     float s, c;          /* Kahan sum and compensation */
     uint32_t dcnt, cnt;  /* density visits, list entries */
@@ -64,7 +66,7 @@ struct DensityAcc {
 
     template <bool LIST>
     __device__ __forceinline__ void visit(float4 q, uint32_t j, float px, float py, float pz, float scale, float h2,
-                                          uint32_t self, uint32_t *lp, uint32_t cap)
+                                          uint32_t *lp, uint32_t cap)
     {
         const float dx = fmaf(-q.x, scale, px), dy = fmaf(-q.y, scale, py), dz = fmaf(-q.z, scale, pz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
@@ -76,7 +78,7 @@ struct DensityAcc {
             c = __fsub_rn(__fsub_rn(u, s), y);
             s = u;
             dcnt++;
-            if (LIST && j != self) {
+            if (LIST) {
                 q0 = q1;
                 q1 = q2;
                 q2 = q3;
