@@ -90,7 +90,10 @@ World::~World()
     if (ev_fluid_ready) cudaEventDestroy(ev_fluid_ready);
     if (ev_rb_done) cudaEventDestroy(ev_rb_done);
     if (ev_bodies_done) cudaEventDestroy(ev_bodies_done);
+    if (ev_io_fork) cudaEventDestroy(ev_io_fork);
+    if (ev_vel_in) cudaEventDestroy(ev_vel_in);
     if (stream2) cudaStreamDestroy(stream2);
+    if (stream3) cudaStreamDestroy(stream3);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -507,6 +510,9 @@ int World::init_stream(cudaStream_t st)
     CK(cudaEventCreateWithFlags(&ev_fluid_ready, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_rb_done, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_bodies_done, cudaEventDisableTiming));
+    CK(cudaStreamCreateWithFlags(&stream3, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ev_io_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_vel_in, cudaEventDisableTiming));
     return FG_OK;
 }
 
@@ -648,6 +654,16 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         CK0(cudaStreamWaitEvent(stream2, ev_fork, 0));
         enqueue_rb_grid(stream2, nullptr, launches);
     }
+    /* end-to-end step: the velocities upload on a third stream while the
+     * positions upload and the hash and sort run; the reorder waits for them */
+    const size_t iob = 16 * (size_t)n;
+    if (cur_io && iob) {
+        CK0(cudaEventRecord(ev_io_fork, stream));
+        CK0(cudaStreamWaitEvent(stream3, ev_io_fork, 0));
+        CK0(cudaMemcpyAsync(vel, cur_io->hv, iob, cudaMemcpyHostToDevice, stream3));
+        CK0(cudaEventRecord(ev_vel_in, stream3));
+        CK0(cudaMemcpyAsync(pos, cur_io->hp, iob, cudaMemcpyHostToDevice, stream));
+    }
     if (stages & FG_STAGE_HASH) {
         mark(0, 0);
         launch_hash(L, pos, keys_u, nullptr);
@@ -660,6 +676,7 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         mark(1, 1);
         launches += 3 * radix_passes(key_bits, digit_bits);
     }
+    if (cur_io && iob) CK0(cudaStreamWaitEvent(stream, ev_vel_in, 0));
     if (stages & FG_STAGE_RANGES) {
         mark(2, 0);
         cudaMemsetAsync(start, 0xff, 4 * (size_t)total_buckets, stream);
@@ -743,6 +760,10 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         mark(7, 1);
         launches += body_launches();
     }
+    if (cur_io && iob) {
+        CK0(cudaMemcpyAsync(cur_io->op, pos, iob, cudaMemcpyDeviceToHost, stream));
+        CK0(cudaMemcpyAsync(cur_io->ov, vel, iob, cudaMemcpyDeviceToHost, stream));
+    }
     return launches;
 }
 
@@ -791,12 +812,13 @@ int World::set_list_cap(uint32_t slots)
 int World::graph_for_current(cudaGraphExec_t *out, uint32_t nsteps)
 {
     const uint64_t sig = graph_signature() ^ ((uint64_t)(nsteps & 0xffu) << 56);
+    const StepIO io = cur_io ? *cur_io : StepIO();
     for (auto &g : graphs)
-        if (g.sig == sig) {
+        if (g.sig == sig && g.io == io) {
             *out = g.exec;
             return FG_OK;
         }
-    CachedGraph g{sig, nullptr, nullptr};
+    CachedGraph g{sig, nullptr, nullptr, io};
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     for (uint32_t k = 0; k < nsteps; k++) enqueue_step();
     cudaError_t e = cudaStreamEndCapture(stream, &g.graph);
@@ -816,9 +838,10 @@ int World::graph_for_current(cudaGraphExec_t *out, uint32_t nsteps)
 }
 
 /* Autotuning round: the candidate values of one tunable (rotating among the
- * kernel, kernel 3's block warps and the radix digit width) each run one
- * real step between CUDA events -- the state advances as in any step -- and
- * the fastest value is kept.  A round may span several step() calls. */
+ * kernel, the CTAs per SM of the density/force grids and the radix digit
+ * width) each run one real step between CUDA events -- the state advances as
+ * in any step -- and the fastest value is kept.  A round may span several
+ * step() calls. */
 void World::tune_begin()
 {
     int dims[3], nd = 0;
@@ -908,10 +931,18 @@ bool World::host_boundary(uint64_t s) const
     return false;
 }
 
-int World::step(uint32_t nsteps)
+int World::step(uint32_t nsteps, const StepIO *io)
+{
+    cur_io = io;
+    int r = step_loop(nsteps);
+    cur_io = nullptr;
+    return r;
+}
+
+int World::step_loop(uint32_t nsteps)
 {
     for (uint32_t k = 0; k < nsteps; k++) {
-        if (use_graphs && graph_steps > 1 && !tr.active && !use_order && nsteps - k >= graph_steps &&
+        if (use_graphs && graph_steps > 1 && !cur_io && !tr.active && !use_order && nsteps - k >= graph_steps &&
             !host_boundary(step_count)) {
             bool clear = true;
             for (uint32_t q = 1; q < graph_steps && clear; q++) clear = !host_boundary(step_count + q);
@@ -1111,21 +1142,45 @@ int World::timed_steps(uint32_t nsteps, size_t fbytes, float *ms, uint32_t per_b
     return FG_OK;
 }
 
+static bool is_pinned(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 int World::e2e_steps(uint32_t nsteps, const float *hp, const float *hv, float *op, float *ov, float *ms)
 {
     Events E(2 * (size_t)nsteps);
+    StepIO io;
+    io.hp = hp;
+    io.hv = hv;
+    io.op = op;
+    io.ov = ov;
+    /* pinned buffers: the copies belong to the step (captured with it, the
+     * velocity upload beside the hash and sort); pageable ones are copied
+     * around it */
+    const bool pinned = is_pinned(hp) && is_pinned(hv) && is_pinned(op) && is_pinned(ov);
     const size_t b = 16 * (size_t)n;
     for (uint32_t k = 0; k < nsteps; k++) {
         CK(cudaEventRecord(E.ev[2 * k], stream));
-        if (b) {
-            CK(cudaMemcpyAsync(pos, hp, b, cudaMemcpyHostToDevice, stream));
-            CK(cudaMemcpyAsync(vel, hv, b, cudaMemcpyHostToDevice, stream));
-        }
-        int r = step(1);
-        if (r != FG_OK) return r;
-        if (b) {
-            CK(cudaMemcpyAsync(op, pos, b, cudaMemcpyDeviceToHost, stream));
-            CK(cudaMemcpyAsync(ov, vel, b, cudaMemcpyDeviceToHost, stream));
+        if (pinned) {
+            int r = step(1, &io);
+            if (r != FG_OK) return r;
+        } else {
+            if (b) {
+                CK(cudaMemcpyAsync(pos, hp, b, cudaMemcpyHostToDevice, stream));
+                CK(cudaMemcpyAsync(vel, hv, b, cudaMemcpyHostToDevice, stream));
+            }
+            int r = step(1);
+            if (r != FG_OK) return r;
+            if (b) {
+                CK(cudaMemcpyAsync(op, pos, b, cudaMemcpyDeviceToHost, stream));
+                CK(cudaMemcpyAsync(ov, vel, b, cudaMemcpyDeviceToHost, stream));
+            }
         }
         CK(cudaEventRecord(E.ev[2 * k + 1], stream));
     }

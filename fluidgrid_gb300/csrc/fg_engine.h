@@ -81,6 +81,8 @@ struct World {
     bool own_stream = false;
     cudaStream_t stream2 = nullptr; /* rigid-body branch of a full step */
     cudaEvent_t ev_fork = nullptr, ev_fluid_ready = nullptr, ev_rb_done = nullptr, ev_bodies_done = nullptr;
+    cudaStream_t stream3 = nullptr; /* velocity upload of an end-to-end step */
+    cudaEvent_t ev_io_fork = nullptr, ev_vel_in = nullptr;
     void enqueue_rb_grid(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches);
     void enqueue_rb_contact(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches);
     void enqueue_bodies(cudaStream_t st, float4 *vf);
@@ -91,10 +93,19 @@ struct World {
     bool fused_integrate = true;
     bool use_graphs = true;
     /* one instantiated step graph per configuration signature */
+    /* host buffers of an end-to-end step: the positions and velocities it
+     * uploads before and downloads after (16 bytes per particle each) */
+    struct StepIO {
+        const void *hp = nullptr, *hv = nullptr;
+        void *op = nullptr, *ov = nullptr;
+        bool operator==(const StepIO &o) const { return hp == o.hp && hv == o.hv && op == o.op && ov == o.ov; }
+    };
+    const StepIO *cur_io = nullptr; /* set while step() runs an end-to-end step */
     struct CachedGraph {
         uint64_t sig;
         cudaGraph_t graph;
         cudaGraphExec_t exec;
+        StepIO io;
     };
     std::vector<CachedGraph> graphs;
     uint64_t graph_signature() const;
@@ -158,7 +169,8 @@ struct World {
     uint32_t enqueue_step(cudaEvent_t *stage_events = nullptr);
     uint32_t *flush_buf = nullptr;
     size_t flush_bytes = 0;
-    int step(uint32_t nsteps);
+    int step(uint32_t nsteps, const StepIO *io = nullptr);
+    int step_loop(uint32_t nsteps);
     uint32_t launches_per_step();
     int check();
     int sync();
