@@ -790,7 +790,7 @@ uint64_t World::graph_signature() const
 int World::set_list_cap(uint32_t slots)
 {
     if (slots < 1 || slots > FG_LIST_CAP_MAX) return FG_E_INVALID;
-    slots = (slots + 3u) & ~3u; /* lists are stored four entries at a time */
+    slots = (slots + 3u) & ~3u; /* the force pass reads lists four entries at a time */
     if (slots > list_cap_alloc) {
         CK(cudaStreamSynchronize(stream));
         const size_t N = std::max<uint64_t>(cap.particles, 1);

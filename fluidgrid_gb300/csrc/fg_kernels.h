@@ -74,11 +74,12 @@ struct TargetOrder {
 /* ---- SPH (fg_sph.cu) ---- */
 
 /* In-range neighbour lists recorded by the density pass and consumed by the
- * force pass: the force pass's neighbours (l <= h, self excluded, duplicate
- * bucket visits kept) in the bucket walk's order.  Target slot t owns
- * idx[t * cap, (t + 1) * cap), cap a multiple of 4, written and read four
- * entries (16 bytes) at a time, so each 32-byte sector is completed by two
- * back-to-back stores of one thread instead of eight scattered 4-byte ones.
+ * force pass: every in-range visit (l <= h, the target's own entries and
+ * duplicate bucket visits kept) in the bucket walk's order; the force pass
+ * skips j == i.  Target slot t owns idx[t * cap, (t + 1) * cap), cap a
+ * multiple of 4.  The density pass writes two entries (8 bytes) at a time,
+ * so a 32-byte sector is completed by four stores of one thread rather than
+ * eight scattered 4-byte ones; the force pass reads four at a time.
  * cnt[t] may exceed cap; then the force pass re-walks the buckets.
  * rec[2i] = (x, y, z, rho_i), rec[2i+1] = (vx, vy, vz, P_i): one 32-byte
  * sector per neighbour gather. */

@@ -49,19 +49,19 @@ __device__ __forceinline__ void fg_walk27(float px, float py, float pz, const Fg
  * reference's l < h sum) and the force pass's neighbour list (every visit
  * with l <= h, the target's own entries included: testing j != i in the
  * force pass, which waits on memory, is cheaper than in this issue-bound
- * branch), buffered in registers and stored four entries at a time.  Every
- * operation is rounded on its own, so any kernel that visits the same
- * candidates in the same order produces the same bits. */
+ * branch), stored two entries (8 bytes) at a time.  Every operation is
+ * rounded on its own, so any kernel that visits the same candidates in the
+ * same order produces the same bits. */
 struct DensityAcc {
     float s, c;          /* Kahan sum and compensation */
     uint32_t dcnt, cnt;  /* density visits, list entries */
-    uint32_t q0, q1, q2, q3; /* the last list entries not yet stored */
+    uint32_t q2, q3;     /* the last two list entries (q3 the newest) */
 
     __device__ __forceinline__ void init()
     {
         s = c = 0.0f;
         dcnt = cnt = 0;
-        q0 = q1 = q2 = q3 = 0;
+        q2 = q3 = 0;
     }
 
     template <bool LIST>
@@ -79,26 +79,18 @@ struct DensityAcc {
             s = u;
             dcnt++;
             if (LIST) {
-                q0 = q1;
-                q1 = q2;
                 q2 = q3;
                 q3 = j;
                 cnt++;
-                if ((cnt & 3u) == 0u && cnt <= cap)
-                    *reinterpret_cast<uint4 *>(lp + cnt - 4u) = make_uint4(q0, q1, q2, q3);
+                if ((cnt & 1u) == 0u && cnt <= cap) *reinterpret_cast<uint2 *>(lp + cnt - 2u) = make_uint2(q2, q3);
             }
         }
     }
 
-    /* store the last 1..3 entries (they sit in q3, (q2, q3) or (q1, q2, q3)) */
+    /* store an odd last entry (q3), zero-padded to 8 bytes */
     __device__ __forceinline__ void flush(uint32_t *lp, uint32_t cap) const
     {
-        if ((cnt & 3u) && cnt < cap) {
-            const uint32_t r = cnt & 3u;
-            const uint4 t = r == 1u ? make_uint4(q3, 0u, 0u, 0u)
-                                    : (r == 2u ? make_uint4(q2, q3, 0u, 0u) : make_uint4(q1, q2, q3, 0u));
-            *reinterpret_cast<uint4 *>(lp + (cnt & ~3u)) = t;
-        }
+        if ((cnt & 1u) && cnt < cap) *reinterpret_cast<uint2 *>(lp + cnt - 1u) = make_uint2(q3, 0u);
     }
 };
 
