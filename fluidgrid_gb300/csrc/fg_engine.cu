@@ -30,6 +30,9 @@
 
 namespace fg {
 
+/* One 32-bit device word set in stream order. */
+__global__ void k_set_u32(uint32_t *p, uint32_t v) { *p = v; }
+
 static thread_local std::string g_err;
 
 void set_error(const char *what, cudaError_t e)
@@ -280,7 +283,8 @@ int World::reserve(const Capacity &c)
     if ((r = A((void **)&rs.hist, 4 * radix_hist_words((uint32_t)M)))) return r;
     if (!list_cap_alloc) list_cap_alloc = FG_LIST_CAP_DEFAULT;
     if ((r = A((void **)&nbr.idx, 4 * (size_t)list_cap_alloc * N))) return r;
-    nbr.cap = list_cap_alloc;
+    nbr.stride = list_cap_alloc;
+    list_cap = list_cap_alloc;
     if ((r = A((void **)&nbr.cnt, 4 * N))) return r;
     if ((r = A((void **)&nbr.rec, 32 * N))) return r;
     if ((r = A((void **)&runs, 4 * N))) return r;
@@ -292,6 +296,9 @@ int World::reserve(const Capacity &c)
     pair_counter = (unsigned long long *)(status_d + 8); /* 8-byte aligned slots of the status block */
     overflow_counter = (unsigned long long *)(status_d + 10);
     max_count = status_d + 12;
+    list_cap_d = status_d + 13;
+    nbr.cap = list_cap_d;
+    k_set_u32<<<1, 1, 0, stream>>>(list_cap_d, list_cap);
     nbr.max_count = max_count;
     nbr.overflow = overflow_counter;
     CK(cudaMemsetAsync(dp, 0, 8 * N, stream));
@@ -784,28 +791,40 @@ uint64_t World::graph_signature() const
     return (uint64_t)((stages & 0xffu) | (fused_integrate ? 0x100u : 0u) | (digit_bits << 9) |
                       (use_list ? 0x10000u : 0u) | ((use_order && order_valid) ? 0x20000u : 0u) |
                       (use_cc ? 0x40000u : 0u) | ((ctas_per_sm & 0x7fu) << 20)) |
-           ((uint64_t)nbr.cap << 32);
+           ((uint64_t)nbr.stride << 32);
 }
 
+/* The capacity is a device word the kernels read, so changing it within the
+ * allocation leaves every captured graph valid.  A capacity beyond the
+ * allocation reallocates the lists with 1.5x headroom (the captured graphs
+ * hold the old pointer and stride and are dropped), so a growing scene
+ * reallocates a few times rather than at every capacity check. */
 int World::set_list_cap(uint32_t slots)
 {
     if (slots < 1 || slots > FG_LIST_CAP_MAX) return FG_E_INVALID;
     slots = (slots + 3u) & ~3u; /* the force pass reads lists four entries at a time */
     if (slots > list_cap_alloc) {
+        const uint32_t grown = ((list_cap_alloc + list_cap_alloc / 2u) + 31u) & ~31u;
+        const uint32_t stride = std::max(slots, std::min(grown, FG_LIST_CAP_MAX));
         CK(cudaStreamSynchronize(stream));
         const size_t N = std::max<uint64_t>(cap.particles, 1);
         uint32_t *p = nullptr;
-        CK(cudaMalloc(&p, 4 * (size_t)slots * N));
-        CK(cudaMemsetAsync(p, 0, 4 * (size_t)slots * N, stream));
+        CK(cudaMalloc(&p, 4 * (size_t)stride * N));
+        CK(cudaMemsetAsync(p, 0, 4 * (size_t)stride * N, stream));
         for (auto &a : allocs)
             if (a == (void *)nbr.idx) a = p;
         cudaFree(nbr.idx);
-        device_bytes += 4 * (size_t)(slots - list_cap_alloc) * N;
+        device_bytes += 4 * (size_t)(stride - list_cap_alloc) * N;
         nbr.idx = p;
-        list_cap_alloc = slots;
+        nbr.stride = stride;
+        list_cap_alloc = stride;
         drop_graphs(); /* every captured step holds the old list pointer */
     }
-    nbr.cap = slots;
+    if (slots != list_cap) {
+        list_cap = slots;
+        k_set_u32<<<1, 1, 0, stream>>>(list_cap_d, list_cap);
+        CK(cudaGetLastError());
+    }
     return FG_OK;
 }
 
@@ -856,7 +875,7 @@ void World::tune_begin()
             if (tune_kernels & (1u << k)) tr.cand[tr.ncand++] = k;
     } else if (tr.dim == 1) {
         /* CTAs per SM of the 128-thread density/force grids */
-        const int v[3] = {8, 16, 64};
+        const int v[3] = {16, 32, 64};
         for (int k = 0; k < 3; k++) tr.cand[tr.ncand++] = v[k];
     } else {
         for (int v = 6; v <= 8; v++) tr.cand[tr.ncand++] = v;
@@ -916,9 +935,9 @@ int World::check_list_cap()
     CK(cudaMemcpyAsync(&mx, max_count, 4, cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
     CK(cudaMemsetAsync(max_count, 0, 4, stream));
-    if (mx <= nbr.cap) return FG_OK;
+    if (mx <= list_cap) return FG_OK;
     const uint32_t want = std::min<uint32_t>(((mx + mx / 8u) + 31u) & ~31u, FG_LIST_CAP_MAX);
-    if (want <= nbr.cap) return FG_OK;
+    if (want <= list_cap) return FG_OK;
     return set_list_cap(want);
 }
 
@@ -1578,7 +1597,7 @@ int fg_world_get_option(const fg_world *w, int option, int *value)
     case FG_OPT_KERNEL: *value = W->current_kernel(); return FG_OK;
     case FG_OPT_AUTOTUNE_PERIOD: *value = (int)W->tune_period; return FG_OK;
     case FG_OPT_AUTOTUNE_KERNELS: *value = (int)W->tune_kernels; return FG_OK;
-    case FG_OPT_LIST_CAP: *value = (int)W->nbr.cap; return FG_OK;
+    case FG_OPT_LIST_CAP: *value = (int)W->list_cap; return FG_OK;
     case FG_OPT_LIST_AUTOGROW: *value = W->list_autogrow ? 1 : 0; return FG_OK;
     case FG_OPT_GRAPH_STEPS: *value = (int)W->graph_steps; return FG_OK;
     case FG_OPT_CTAS_PER_SM: *value = (int)W->ctas_per_sm; return FG_OK;

@@ -46,12 +46,14 @@ struct World {
     uint32_t *keys_u = nullptr, *keys = nullptr, *ids = nullptr, *start = nullptr, *end = nullptr;
     RadixScratch rs{nullptr, nullptr, nullptr};
     NbrList nbr{nullptr, nullptr, nullptr, 0, nullptr, nullptr}; /* density -> forces neighbour lists */
-    uint32_t list_cap_alloc = 0; /* list slots per particle allocated */
+    uint32_t list_cap_alloc = 0; /* list slots per particle allocated (the stride) */
+    uint32_t list_cap = 0;       /* entries a particle may store (<= list_cap_alloc) */
+    uint32_t *list_cap_d = nullptr; /* the same, in device memory for the kernels */
     uint32_t *inv = nullptr;  /* particle -> sorted index (written by the ranges pass) */
     uint32_t *tord = nullptr; /* spatial target order (particle ids, scene-contiguous) */
     bool use_list = true, use_order = false;
     bool use_cc = false;       /* kernel 2: warp per bucket run, candidates staged in shared memory */
-    uint32_t ctas_per_sm = 0;  /* CTAs per SM of the density/force grids (0 = 16) */
+    uint32_t ctas_per_sm = 0;  /* CTAs per SM of the density/force grids (0 = 64) */
     int set_list_cap(uint32_t cap);
     uint32_t *runs = nullptr;  /* occupied-bucket run heads */
     uint32_t *nruns = nullptr; /* device counter */

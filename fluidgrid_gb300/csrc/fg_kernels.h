@@ -76,8 +76,9 @@ struct TargetOrder {
 /* In-range neighbour lists recorded by the density pass and consumed by the
  * force pass: every in-range visit (l <= h, the target's own entries and
  * duplicate bucket visits kept) in the bucket walk's order; the force pass
- * skips j == i.  Target slot t owns idx[t * cap, (t + 1) * cap), cap a
- * multiple of 4.  The density pass writes two entries (8 bytes) at a time,
+ * skips j == i.  Target slot t owns idx[t * stride, (t + 1) * stride) and
+ * stores at most cap entries there; cap lives in device memory, so the host
+ * changes it between steps without touching a captured graph.  The density pass writes two entries (8 bytes) at a time,
  * so a 32-byte sector is completed by four stores of one thread rather than
  * eight scattered 4-byte ones; the force pass reads four at a time.
  * cnt[t] may exceed cap; then the force pass re-walks the buckets.
@@ -87,7 +88,8 @@ struct NbrList {
     uint32_t *idx;
     uint32_t *cnt;
     float4 *rec;
-    uint32_t cap;
+    uint32_t stride;              /* slots per target in idx, a multiple of 4 */
+    const uint32_t *cap;          /* device word: entries a target may store (<= stride) */
     uint32_t *max_count;          /* optional: atomicMax of cnt */
     unsigned long long *overflow; /* optional: targets with cnt > cap */
 };

@@ -177,15 +177,18 @@ int fg_world_set_graphs(fg_world *w, int on);
  *                         multiple of 4 (default 160, at most 2048; values
  *                         round up to a multiple of 4; a particle with more
  *                         in-range visits re-walks its buckets in the force
- *                         pass; a larger value reallocates the lists; setting
- *                         it turns FG_OPT_LIST_AUTOGROW off)
+ *                         pass; a value beyond the allocation reallocates
+ *                         the lists with 1.5x headroom, one within it changes
+ *                         nothing but the limit; setting it turns
+ *                         FG_OPT_LIST_AUTOGROW off)
  *   FG_OPT_LIST_AUTOGROW  kernel 1: 1 = every 25 steps grow the capacity to
  *                         1.125x the largest in-range count seen (default)
  *   FG_OPT_GRAPH_STEPS    steps captured in one CUDA graph launch (1..64,
  *                         default 1); such a launch never spans an
  *                         autotuning round or a list capacity check
  *   FG_OPT_CTAS_PER_SM    kernels 0/1: CTAs per SM of the persistent
- *                         128-thread density/force grids (0 = 16)
+ *                         128-thread density/force grids (0 = 64; the
+ *                         autotuner tries 16, 32 and 64)
  *   FG_OPT_AUTOTUNE_TILES bit mask of the tunables the autotuner varies:
  *                         1 = CTAs per SM, 2 = radix digit width (default 3)
  * Kernels 0 and 1 (with either target order) produce bit-identical states;
