@@ -29,6 +29,9 @@ void launch_hash(const Launch &L, const float4 *pos, uint32_t *keys, uint32_t *i
 void launch_hash_with_offset(const Launch &L, const float4 *local, const float4 *cm, const float4 *q,
                              float4 *world, uint32_t *keys, uint32_t *ids, int *aabb /* 6 ints per scene or null */);
 
+/* keys per radix tile (one CTA of the upsweep/downsweep); the histogram
+ * holds 256 counts per tile plus 256 digit totals */
+#define FG_RS_TILE 4096u
 struct RadixScratch {
     uint32_t *keys_alt;
     uint32_t *vals_alt;

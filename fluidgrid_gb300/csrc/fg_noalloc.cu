@@ -33,8 +33,9 @@
 
 #define FG_NOALLOC_MAX_PAIRS (1u << 20)
 /* keys + values ping-pong buffers, then the radix tile histograms
- * (256 digits x 256 tiles of 4096 keys) and the 256 digit totals */
-#define FG_NOALLOC_HIST_WORDS (256u * (FG_NOALLOC_MAX_PAIRS / 4096u) + 256u)
+ * (256 digits x one count per tile of FG_RS_TILE keys) and the 256 digit
+ * totals */
+#define FG_NOALLOC_HIST_WORDS (256u * ((FG_NOALLOC_MAX_PAIRS + FG_RS_TILE - 1u) / FG_RS_TILE) + 256u)
 #define FG_NOALLOC_WORDS (2u * FG_NOALLOC_MAX_PAIRS + FG_NOALLOC_HIST_WORDS)
 
 static __device__ __align__(256) uint32_t g_noalloc_scratch[FG_NOALLOC_WORDS];
