@@ -136,7 +136,7 @@ void launch_hash_with_offset(const Launch &L, const float4 *local, const float4 
  * items are ranked k-major, lane-minor), so each pass is stable. */
 
 #define RS_THREADS 256
-#define RS_ITEMS 16
+#define RS_ITEMS 8
 #define RS_TILE (RS_THREADS * RS_ITEMS)
 static_assert(RS_TILE == FG_RS_TILE, "scratch sizes elsewhere assume FG_RS_TILE keys per tile");
 #define RS_RADIX 256

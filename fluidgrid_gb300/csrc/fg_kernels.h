@@ -31,7 +31,7 @@ void launch_hash_with_offset(const Launch &L, const float4 *local, const float4 
 
 /* keys per radix tile (one CTA of the upsweep/downsweep); the histogram
  * holds 256 counts per tile plus 256 digit totals */
-#define FG_RS_TILE 4096u
+#define FG_RS_TILE 2048u
 struct RadixScratch {
     uint32_t *keys_alt;
     uint32_t *vals_alt;
