@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(FG_CHUNK, 16) k_density(const FgWork *__restri
             list.rec[2 * i] = make_float4(p.x, p.y, p.z, d.x);
             list.rec[2 * i + 1] = make_float4(v.x, v.y, v.z, d.y);
         }
-        const uint32_t cnt = acc.cnt, dcnt = acc.dcnt;
+        const uint32_t cnt = acc.cnt, dcnt = LIST ? acc.cnt : acc.dcnt;
         if (LIST && valid) list.cnt[tpos] = cnt;
         pc += dcnt;
         mx = max(mx, cnt);

@@ -54,7 +54,7 @@ __device__ __forceinline__ void fg_walk27(float px, float py, float pz, const Fg
  * same order produces the same bits. */
 struct DensityAcc {
     float s, c;          /* Kahan sum and compensation */
-    uint32_t dcnt, cnt;  /* density visits, list entries */
+    uint32_t dcnt, cnt;  /* density visits (without a list), list entries */
     uint32_t q2, q3;     /* the last two list entries (q3 the newest) */
 
     __device__ __forceinline__ void init()
@@ -77,7 +77,7 @@ struct DensityAcc {
             const float u = __fadd_rn(s, y);
             c = __fsub_rn(__fsub_rn(u, s), y);
             s = u;
-            dcnt++;
+            if (!LIST) dcnt++; /* with a list every visit is an entry: cnt counts them */
             if (LIST) {
                 q2 = q3;
                 q3 = j;
