@@ -415,7 +415,9 @@ def run_ours(args, rank, world, local):
                          "bytes_per_particle": per_p, "fp32": fp32},
             "cpu_baseline": ({k: v for k, v in cpu.items() if k != "pairs_per_step"} if cpu else None),
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 32 * n,
-                    "d2h_bytes_per_step": 32 * n},
+                    "d2h_bytes_per_step": 32 * n, "ms_per_step": e2e_ms / K,
+                    "step_ms": {"p50": float(np.percentile(ems, 50)), "p99": float(np.percentile(ems, 99)),
+                                "max": float(ems.max())}},
             "gpu_launches": launches * K + K,
             "clocks": clk,
             "forms": forms,
