@@ -18,12 +18,14 @@
  * One thread per particle in sorted order: neighbouring lanes share cells,
  * so neighbour loads broadcast from L1 and sorted float4 loads coalesce.
  * In the world pipeline the density pass is the only one that walks the
- * ~216 candidates of the 27 buckets: it stages each particle's in-range
- * neighbours (in visit order, duplicates included) in shared memory and
- * writes them out coalesced, together with a packed 32-byte record per
- * particle.  The force pass then loops over ~30 listed neighbours per
- * particle with all lanes busy, instead of re-walking 216 candidates where
- * almost every warp iteration would run the pair math for a few lanes. */
+ * ~216 candidates of the 27 buckets (~1,000 once the block compresses): it
+ * records each particle's in-range visits (in visit order, duplicates and
+ * the particle itself included) in the particle's own list, buffered in
+ * registers and stored two entries at a time, together with a packed
+ * 32-byte record per particle.  The force pass then loops over the ~30-110
+ * listed neighbours per particle with all lanes busy, one 256-bit record
+ * load each, instead of re-walking the candidates where almost every warp
+ * iteration would run the pair math for a few lanes. */
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
