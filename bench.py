@@ -264,12 +264,14 @@ def run_batched(steps=1000, warmup=10, plain_sample=64):
             "autotune": tuning}
 
 
-def run_served(duration=20.0, rate=200.0, budget=120 << 30, max_particles=0, seed=0x5EED, label="served"):
+def run_served(duration=20.0, rate=200.0, budget=120 << 30, max_particles=0, seed=0x5EED, label="served",
+               pipeline_depth=2):
     """Served form: Poisson arrivals of dam-break requests (fluid counts
     log-uniform in [4,096, 524,288], 0-4 rigid boxes of 1,024 spheres, step
     counts uniform in [100, 2000]) for `duration` seconds of wall time into a
     continuous-batching server with an HBM budget; every server step admits
-    what fits and advances every resident scene."""
+    what fits and advances every resident scene, leaving up to
+    `pipeline_depth` steps running while the host prepares the next."""
     from fluidgrid_gb300 import scenes
     from fluidgrid_gb300.server import Server
     pool = scenes.served_templates(seed=seed)
@@ -278,7 +280,7 @@ def run_served(duration=20.0, rate=200.0, budget=120 << 30, max_particles=0, see
     arrivals = arrivals[arrivals < duration]
     picks = rng.integers(0, len(pool), len(arrivals))
     nsteps = rng.integers(100, 2001, len(arrivals))
-    srv = Server(budget_bytes=budget, max_particles=max_particles)
+    srv = Server(budget_bytes=budget, max_particles=max_particles, pipeline_depth=pipeline_depth)
     ids = []
     infos = []
     t0 = time.perf_counter()
@@ -300,7 +302,8 @@ def run_served(duration=20.0, rate=200.0, budget=120 << 30, max_particles=0, see
     step_ms = [i["step_ms"] for i in infos if i["active_particles"]]
     wall_ms = [i["wall_ms"] for i in infos if i["active_particles"]]
     return {"workload": label, "duration_s": duration, "arrival_rate_per_s": rate, "budget_bytes": budget,
-            "max_particles_per_step": max_particles, "submitted": len(ids), "admitted": len(admitted),
+            "max_particles_per_step": max_particles, "pipeline_depth": pipeline_depth,
+            "submitted": len(ids), "admitted": len(admitted),
             "completed": len(done), "queued_at_end": st["queued"], "server_steps": st["steps"],
             "value": st["particle_steps"] / elapsed, "unit": "particle-steps/s",
             "step_latency_ms": {"p50": pct(step_ms, 50), "p99": pct(step_ms, 99)},

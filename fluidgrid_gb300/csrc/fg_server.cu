@@ -51,6 +51,8 @@ struct Request {
     std::vector<float> out_pos, out_vel;     /* final state */
 };
 
+#define FG_SERVER_RING 16 /* pipeline_depth is clamped below this */
+
 struct Server {
     fg_server_config cfg;
     cudaStream_t stream = nullptr;
@@ -63,7 +65,10 @@ struct Server {
     uint64_t next_id = 1;
     size_t resident = 0;
     uint64_t resident_particles = 0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    /* step events: slot k % FG_SERVER_RING brackets step k */
+    cudaEvent_t ev0[FG_SERVER_RING] = {}, ev1[FG_SERVER_RING] = {};
+    uint64_t issued = 0, waited = 0; /* steps enqueued / steps whose end was waited for */
+    float last_ms = 0.0f;           /* device time of the newest step waited for */
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
     uint64_t steps = 0, particle_steps = 0;
     uint32_t stable_steps = 0; /* steps since the last re-layout */
@@ -75,8 +80,10 @@ struct Server {
     ~Server()
     {
         w.reset();
-        if (ev0) cudaEventDestroy(ev0);
-        if (ev1) cudaEventDestroy(ev1);
+        for (int k = 0; k < FG_SERVER_RING; k++) {
+            if (ev0[k]) cudaEventDestroy(ev0[k]);
+            if (ev1[k]) cudaEventDestroy(ev1[k]);
+        }
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
     bool layout_current() const
@@ -89,6 +96,17 @@ struct Server {
     int relayout();
     int retire_finished();
     int step(fg_server_step_info *info);
+    /* wait until at most `depth` enqueued steps are unfinished */
+    int drain(uint64_t depth)
+    {
+        while (issued - waited > depth) {
+            const int k = (int)(waited % FG_SERVER_RING);
+            CK(cudaEventSynchronize(ev1[k]));
+            CK(cudaEventElapsedTime(&last_ms, ev0[k], ev1[k]));
+            waited++;
+        }
+        return FG_OK;
+    }
 };
 
 /* Device bytes one scene adds to a world at list capacity list_cap. */
@@ -110,6 +128,7 @@ int Server::relayout()
     for (size_t o = 0; o < laid_out.size(); o++) where[laid_out[o]] = (uint32_t)o;
     std::vector<FgScene> old_scenes;
     if (w) old_scenes.assign(w->scenes_h.begin(), w->scenes_h.begin() + w->nscenes);
+    if (drain(0) != FG_OK) return FG_E_CUDA;
     if (w) CK(cudaStreamSynchronize(stream));
     /* body motion of continuing scenes goes through the host (small) */
     std::vector<double> hx, hv, hq, hL;
@@ -244,6 +263,7 @@ int Server::retire_finished()
     for (auto *q : active)
         if (q->steps_done >= q->steps_total) any = true;
     if (!any) return FG_OK;
+    if (drain(0) != FG_OK) return FG_E_CUDA;
     CK(cudaStreamSynchronize(stream));
     std::vector<Request *> keep;
     for (size_t s = 0; s < active.size(); s++) {
@@ -303,12 +323,17 @@ int Server::step(fg_server_step_info *info)
         /* a layout that just changed runs uncaptured; a stable one replays
          * its captured step */
         w->use_graphs = cfg.use_graphs && stable_steps >= 1;
-        CK(cudaEventRecord(ev0, w->stream));
+        /* the slot about to be reused must hold a finished step */
+        if (drain(FG_SERVER_RING - 1) != FG_OK) return FG_E_CUDA;
+        const int k = (int)(issued % FG_SERVER_RING);
+        CK(cudaEventRecord(ev0[k], w->stream));
         int r = w->step(1);
         if (r != FG_OK) return r;
-        CK(cudaEventRecord(ev1, w->stream));
-        CK(cudaEventSynchronize(ev1));
-        CK(cudaEventElapsedTime(&ms, ev0, ev1));
+        CK(cudaEventRecord(ev1[k], w->stream));
+        issued++;
+        const int depth = std::min(std::max(cfg.pipeline_depth, 0), FG_SERVER_RING - 1);
+        if (drain((uint64_t)depth) != FG_OK) return FG_E_CUDA;
+        ms = last_ms;
         adv = w->n;
     }
     for (auto *q : active) q->steps_done++;
@@ -357,8 +382,10 @@ int fg_server_create(const fg_server_config *cfg, fg_stream_t stream, fg_server 
         CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
         s->own_stream = true;
     }
-    CK(cudaEventCreate(&s->ev0));
-    CK(cudaEventCreate(&s->ev1));
+    for (int k = 0; k < FG_SERVER_RING; k++) {
+        CK(cudaEventCreate(&s->ev0[k]));
+        CK(cudaEventCreate(&s->ev1[k]));
+    }
     *out = (fg_server *)s.release();
     return FG_OK;
 }

@@ -11,7 +11,7 @@ from ._ffi import check
 
 class Server:
     def __init__(self, budget_bytes=120 << 30, max_particles=0, max_admit_per_step=0, use_graphs=True,
-                 grow_via_host=False, stream=None):
+                 grow_via_host=False, stream=None, pipeline_depth=0):
         self.L = _ffi.load()
         cfg = _ffi.fg_server_config()
         self.L.fg_server_config_defaults(ctypes.byref(cfg))
@@ -20,6 +20,7 @@ class Server:
         cfg.max_admit_per_step = int(max_admit_per_step)
         cfg.use_graphs = 1 if use_graphs else 0
         cfg.grow_via_host = 1 if grow_via_host else 0
+        cfg.pipeline_depth = int(pipeline_depth)
         h = ctypes.c_void_p()
         check(self.L.fg_server_create(ctypes.byref(cfg), ctypes.c_void_p(stream) if stream else None,
                                       ctypes.byref(h)), "fg_server_create")

@@ -288,7 +288,10 @@ typedef struct fg_server_config {
     int use_graphs;               /* replay captured steps while the resident set is stable */
     int grow_via_host;            /* 1: when the world grows, always park the state on the host
                                      (otherwise only when both worlds would not fit) */
-    int reserved[2];
+    int pipeline_depth;           /* steps fg_server_step may leave running on the device (0 =
+                                     return after each step finishes); a change of the resident
+                                     set, a retirement or a result waits for all of them */
+    int reserved;
 } fg_server_config;
 enum { FG_REQ_QUEUED = 0, FG_REQ_ACTIVE = 1, FG_REQ_DONE = 2 };
 typedef struct fg_server_step_info {
@@ -297,7 +300,8 @@ typedef struct fg_server_step_info {
     uint32_t finished;        /* scenes that reached their step count */
     uint32_t queued;          /* requests still waiting */
     uint64_t active_particles;
-    float step_ms;            /* device time of the step (CUDA events) */
+    float step_ms;            /* device time of the step (CUDA events); with pipeline_depth > 0,
+                                 of the newest step that has finished (0 if none has) */
     float pad_;
     double wall_ms;           /* host time of fg_server_step (admission, layout, step, retirement) */
     size_t resident_bytes;

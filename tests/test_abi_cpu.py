@@ -54,8 +54,9 @@ int main(void) {
   printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(fg_scene_desc), offsetof(fg_scene_desc, bodies),
          offsetof(fg_scene_desc, rb_volume_max), sizeof(fg_body_desc), offsetof(fg_body_desc, inv_inertia),
          sizeof(fgr_common_fluid_params), offsetof(fgr_common_fluid_params, fluid_to_srb_relation));
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(fg_server_config),
-         offsetof(fg_server_config, use_graphs), sizeof(fg_server_step_info),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(fg_server_config),
+         offsetof(fg_server_config, use_graphs), offsetof(fg_server_config, pipeline_depth),
+         sizeof(fg_server_step_info),
          offsetof(fg_server_step_info, wall_ms), offsetof(fg_server_step_info, resident_bytes),
          sizeof(fg_request_info), offsetof(fg_request_info, submit_s), offsetof(fg_request_info, resident_bytes),
          sizeof(fg_server_stats_info), offsetof(fg_server_stats_info, device_bytes));
@@ -79,7 +80,7 @@ def test_struct_layouts_match_ctypes():
             ctypes.sizeof(C), C.fluid_to_srb_relation.offset]
     SC, SI, RI, ST = (_ffi.fg_server_config, _ffi.fg_server_step_info, _ffi.fg_request_info,
                       _ffi.fg_server_stats_info)
-    want += [ctypes.sizeof(SC), SC.use_graphs.offset, ctypes.sizeof(SI), SI.wall_ms.offset,
+    want += [ctypes.sizeof(SC), SC.use_graphs.offset, SC.pipeline_depth.offset, ctypes.sizeof(SI), SI.wall_ms.offset,
              SI.resident_bytes.offset, ctypes.sizeof(RI), RI.submit_s.offset, RI.resident_bytes.offset,
              ctypes.sizeof(ST), ST.device_bytes.offset]
     assert got == want

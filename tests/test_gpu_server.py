@@ -45,10 +45,14 @@ def _run(server, ss, steps, arrive):
     return ids, max_active
 
 
-@pytest.mark.parametrize("graphs,via_host", [(True, False), (False, False), (True, True)])
-def test_results_equal_scene_alone(graphs, via_host):
+@pytest.mark.parametrize("graphs,via_host,depth", [(True, False, 0), (False, False, 0), (True, True, 0),
+                                                   (True, False, 3), (False, True, 2)])
+def test_results_equal_scene_alone(graphs, via_host, depth):
+    """Every request's result equals its scene stepped alone: with and without
+    graph replay, through host-parked growth, and with fg_server_step leaving
+    up to `depth` steps running on the device."""
     ss, steps, arrive = _mix()
-    with Server(budget_bytes=64 << 30, use_graphs=graphs, grow_via_host=via_host) as srv:
+    with Server(budget_bytes=64 << 30, use_graphs=graphs, grow_via_host=via_host, pipeline_depth=depth) as srv:
         ids, max_active = _run(srv, ss, steps, arrive)
         assert max_active >= 3  # the scenes really overlapped on the device
         for s, rid in ids.items():
