@@ -84,10 +84,7 @@ World::~World()
     if (diag_out) cudaFree(diag_out);
     for (auto &e : tr.ev)
         if (e) cudaEventDestroy(e);
-    for (auto &g : graphs) {
-        if (g.exec) cudaGraphExecDestroy(g.exec);
-        if (g.graph) cudaGraphDestroy(g.graph);
-    }
+    drop_graphs();
     for (void *p : allocs) cudaFree(p);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_fluid_ready) cudaEventDestroy(ev_fluid_ready);
@@ -450,7 +447,7 @@ int World::set_layout(const fg_scene_desc *d, uint32_t ns)
         CK(cudaMemcpy(body_first, hbf.data(), 4 * B, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(body_count, hbc.data(), 4 * B, cudaMemcpyHostToDevice));
     }
-    drop_graphs();
+    stale_graphs();
     return FG_OK;
 }
 
@@ -495,11 +492,25 @@ int World::upload_scene(uint32_t s, const fg_scene_desc &d)
 
 void World::drop_graphs()
 {
-    for (auto &g : graphs) {
-        if (g.exec) cudaGraphExecDestroy(g.exec);
-        if (g.graph) cudaGraphDestroy(g.graph);
+    for (auto *v : {&graphs, &stale}) {
+        for (auto &g : *v) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            if (g.graph) cudaGraphDestroy(g.graph);
+        }
+        v->clear();
     }
+}
+
+void World::stale_graphs()
+{
+    for (auto &g : graphs) stale.push_back(g);
     graphs.clear();
+    /* bound the kept set: the oldest go first */
+    while (stale.size() > 32) {
+        if (stale.front().exec) cudaGraphExecDestroy(stale.front().exec);
+        if (stale.front().graph) cudaGraphDestroy(stale.front().graph);
+        stale.erase(stale.begin());
+    }
 }
 
 int World::init_stream(cudaStream_t st)
@@ -818,7 +829,7 @@ int World::set_list_cap(uint32_t slots)
         nbr.idx = p;
         nbr.stride = stride;
         list_cap_alloc = stride;
-        drop_graphs(); /* every captured step holds the old list pointer */
+        stale_graphs(); /* every captured step holds the old list pointer */
     }
     if (slots != list_cap) {
         list_cap = slots;
@@ -844,6 +855,23 @@ int World::graph_for_current(cudaGraphExec_t *out, uint32_t nsteps)
     if (e != cudaSuccess) {
         set_error("cudaStreamEndCapture", e);
         return FG_E_CUDA;
+    }
+    for (size_t k = 0; k < stale.size(); k++) {
+        if (stale[k].sig != sig || !(stale[k].io == io)) continue;
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(stale[k].exec, g.graph, &info) == cudaSuccess) {
+            g.exec = stale[k].exec;
+            cudaGraphDestroy(stale[k].graph);
+            stale.erase(stale.begin() + (long)k);
+            graphs.push_back(g);
+            *out = g.exec;
+            return FG_OK;
+        }
+        cudaGetLastError(); /* another topology (e.g. another radix pass count): instantiate */
+        cudaGraphExecDestroy(stale[k].exec);
+        cudaGraphDestroy(stale[k].graph);
+        stale.erase(stale.begin() + (long)k);
+        break;
     }
     e = cudaGraphInstantiate(&g.exec, g.graph, 0);
     if (e != cudaSuccess) {

@@ -110,6 +110,10 @@ struct World {
         StepIO io;
     };
     std::vector<CachedGraph> graphs;
+    /* graphs whose parameters a layout change or a list reallocation made
+     * stale: a later capture with the same signature updates one in place
+     * (cudaGraphExecUpdate) instead of instantiating a new one */
+    std::vector<CachedGraph> stale;
     uint64_t graph_signature() const;
     int graph_for_current(cudaGraphExec_t *out, uint32_t nsteps = 1);
     uint32_t graph_steps = 1; /* steps per captured graph launch */
@@ -159,7 +163,8 @@ struct World {
     int reserve(const Capacity &c);
     int set_layout(const fg_scene_desc *d, uint32_t ns);
     int upload_scene(uint32_t s, const fg_scene_desc &d);
-    void drop_graphs();
+    void drop_graphs();  /* destroys every captured graph */
+    void stale_graphs(); /* keeps them for in-place updates */
     /* FP64 conservation diagnostics */
     std::vector<uint32_t> work_first_h; /* scene s owns work items [first[s], first[s+1]) */
     uint32_t *diag_first = nullptr;
