@@ -410,7 +410,8 @@ def run_ours(args, rank, world, local):
                        "l2": "flushed before every timed step (256 MiB write)",
                        "parallelism": "replicas" if world > 1 else "single",
                        "autotune": tuning},
-            "latency_ms": {"p50": float(np.percentile(ms_sorted, 50)), "p99": float(np.percentile(ms_sorted, 99))},
+            "latency_ms": {"p50": float(np.percentile(ms_sorted, 50)), "p99": float(np.percentile(ms_sorted, 99)),
+                           "max": float(ms_sorted[-1]), "slowest_steps": [int(W + k) for k in np.argsort(-ms)[:5]]},
             "stages_ms": stages,
             "roofline": {"bound": "hbm", "kernel": "k_forces" if dom == "forces" else "k_density",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
