@@ -238,7 +238,7 @@ size_t World::footprint(const Capacity &c, uint32_t list_cap)
     const size_t M = std::max(P, S);
     size_t b = 0;
     b += P * (16 + 16 + 4 + 4 + 4 + 16 + 16 + 8); /* pos vel keys_u keys ids spos svel dp */
-    b += M * 8 + 4 * radix_hist_words((uint32_t)M); /* sort scratch */
+    b += M * 8 + 4 * radix_hist_words((uint32_t)M) + 4 * onesweep_words((uint32_t)P); /* sort scratch */
     b += P * (4 * (size_t)list_cap + 4 + 32);      /* lists, counts, records */
     b += P * 12;                                    /* runs, inv, tord */
     b += 8 * std::max<uint64_t>(c.buckets, 1);
@@ -278,6 +278,7 @@ int World::reserve(const Capacity &c)
     if ((r = A((void **)&rs.keys_alt, 4 * M))) return r;
     if ((r = A((void **)&rs.vals_alt, 4 * M))) return r;
     if ((r = A((void **)&rs.hist, 4 * radix_hist_words((uint32_t)M)))) return r;
+    if ((r = A((void **)&os_scratch, 4 * onesweep_words((uint32_t)N)))) return r;
     if (!list_cap_alloc) list_cap_alloc = FG_LIST_CAP_DEFAULT;
     if ((r = A((void **)&nbr.idx, 4 * (size_t)list_cap_alloc * N))) return r;
     nbr.stride = list_cap_alloc;
@@ -690,9 +691,14 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
     }
     if (stages & FG_STAGE_SORT) {
         mark(1, 0);
-        radix_sort(keys_u, nullptr, keys, ids, n, key_bits, digit_bits, rs, stream);
+        if (one_pass_sort && onesweep_sort(keys_u, keys, ids, n, key_bits, digit_bits, rs, os_scratch, status_d,
+                                           stream)) {
+            launches += 2 + radix_passes(key_bits, digit_bits);
+        } else {
+            radix_sort(keys_u, nullptr, keys, ids, n, key_bits, digit_bits, rs, stream);
+            launches += 3 * radix_passes(key_bits, digit_bits);
+        }
         mark(1, 1);
-        launches += 3 * radix_passes(key_bits, digit_bits);
     }
     if (cur_io && iob) CK0(cudaStreamWaitEvent(stream, ev_vel_in, 0));
     if (stages & FG_STAGE_RANGES) {
@@ -1053,7 +1059,10 @@ uint32_t World::launches_per_step()
     /* count by enqueueing into a capture-free dry description */
     uint32_t c = 0;
     if (stages & FG_STAGE_HASH) c += 1;
-    if (stages & FG_STAGE_SORT) c += 3 * radix_passes(key_bits, digit_bits);
+    if (stages & FG_STAGE_SORT) {
+        const uint32_t P = radix_passes(key_bits, digit_bits);
+        c += (one_pass_sort && n && P <= 6) ? 2 + P : 3 * P;
+    }
     if (stages & FG_STAGE_RANGES) c += 1; /* + one memset node */
     if (stages & FG_STAGE_DENSITY) c += 1;
     if (nbodies) {
@@ -1115,6 +1124,10 @@ int World::sync()
     uint32_t st = 0;
     CK(cudaMemcpy(&st, status_d, 4, cudaMemcpyDeviceToHost));
     if (st & FG_DEV_NONFINITE) return FG_E_NONFINITE;
+    if (st & FG_DEV_SORT_TIMEOUT) {
+        set_error_msg("a one-pass radix sort gave up waiting on a preceding tile");
+        return FG_E_TIMEOUT;
+    }
     return FG_OK;
 }
 
@@ -1563,6 +1576,7 @@ int fg_world_set_option(fg_world *w, int option, int value)
         if (value < 1 || value > 64) return FG_E_INVALID;
         W->graph_steps = (uint32_t)value;
         return FG_OK;
+    case FG_OPT_ONE_PASS_SORT: W->one_pass_sort = value != 0; return FG_OK;
     case FG_OPT_CTAS_PER_SM:
         if (value < 0 || value > 64) return FG_E_INVALID;
         W->ctas_per_sm = (uint32_t)value;
@@ -1630,6 +1644,7 @@ int fg_world_get_option(const fg_world *w, int option, int *value)
     case FG_OPT_LIST_CAP: *value = (int)W->list_cap; return FG_OK;
     case FG_OPT_LIST_AUTOGROW: *value = W->list_autogrow ? 1 : 0; return FG_OK;
     case FG_OPT_GRAPH_STEPS: *value = (int)W->graph_steps; return FG_OK;
+    case FG_OPT_ONE_PASS_SORT: *value = W->one_pass_sort ? 1 : 0; return FG_OK;
     case FG_OPT_CTAS_PER_SM: *value = (int)W->ctas_per_sm; return FG_OK;
     case FG_OPT_AUTOTUNE_TILES: *value = (int)W->tune_tiles; return FG_OK;
     default: return FG_E_INVALID;

@@ -355,6 +355,230 @@ void radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys
     }
 }
 
+/* ---------------------------------------------------------- onesweep
+ * Stable LSD radix sort with one kernel per digit pass, after one histogram
+ * kernel for all passes (decoupled look-back):
+ *   k_os_hist  global digit counts of every pass (one read of the keys)
+ *   k_os_scan  exclusive digit bases of every pass
+ *   k_os_pass  per tile of RS_TILE keys, taken in launch order through a
+ *              counter: rank the keys in the tile exactly as k_rs_downsweep
+ *              does, publish the tile's per-digit counts, add up the
+ *              preceding tiles' counts by looking back until a tile whose
+ *              inclusive prefix is known, publish this tile's inclusive
+ *              prefix, scatter.
+ * A tile waits only on tiles taken before it, which publish their counts
+ * before they wait themselves, so every wait ends; each wait is bounded all
+ * the same, and one that gives up sets FG_DEV_SORT_TIMEOUT and goes on. */
+#define OS_MAX_PASSES 6
+#define OS_AGG 0x40000000u
+#define OS_INC 0x80000000u
+#define OS_CNT 0x3fffffffu
+#define OS_SPIN_LIMIT (1u << 22)
+#define OS_WINDOW 8
+
+static uint32_t os_tiles(uint32_t n) { return std::max<uint32_t>((n + RS_TILE - 1) / RS_TILE, 1u); }
+
+size_t onesweep_words(uint32_t n)
+{
+    /* status words [pass][tile][digit], digit counts/bases [pass][digit], tile counters */
+    return (size_t)OS_MAX_PASSES * RS_RADIX * os_tiles(n) + (size_t)OS_MAX_PASSES * RS_RADIX + 32;
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_os_hist(const uint32_t *__restrict__ keys, uint32_t n,
+                                                       uint32_t bits, uint32_t db, uint32_t passes,
+                                                       uint32_t *__restrict__ counts)
+{
+    __shared__ uint32_t h[OS_MAX_PASSES][RS_RADIX];
+#pragma unroll
+    for (int p = 0; p < OS_MAX_PASSES; p++) h[p][threadIdx.x] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = __ldg(keys + i);
+        for (uint32_t p = 0; p < passes; p++) {
+            const uint32_t shift = p * db, b = min(db, bits - shift);
+            atomicAdd(&h[p][(k >> shift) & ((1u << b) - 1u)], 1u);
+        }
+    }
+    __syncthreads();
+    for (uint32_t p = 0; p < passes; p++) {
+        const uint32_t v = h[p][threadIdx.x];
+        if (v) atomicAdd(&counts[p * RS_RADIX + threadIdx.x], v);
+    }
+}
+
+/* one CTA per pass: counts -> exclusive digit bases, in place */
+__global__ void __launch_bounds__(RS_THREADS) k_os_scan(uint32_t *__restrict__ counts)
+{
+    __shared__ uint32_t s_warp[RS_WARPS + 1];
+    uint32_t *c = counts + blockIdx.x * RS_RADIX;
+    uint32_t tot;
+    const uint32_t e = rs_block_excl(c[threadIdx.x], s_warp, tot);
+    c[threadIdx.x] = e;
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_os_pass(const uint32_t *__restrict__ kin,
+                                                       const uint32_t *__restrict__ vin,
+                                                       uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
+                                                       uint32_t n, uint32_t shift, uint32_t mask,
+                                                       uint32_t *__restrict__ status,
+                                                       const uint32_t *__restrict__ bases,
+                                                       uint32_t *__restrict__ tile_ctr, uint32_t *__restrict__ err)
+{
+    __shared__ uint32_t s_keys[RS_TILE];
+    __shared__ uint32_t s_vals[RS_TILE];
+    __shared__ uint32_t s_whist[RS_WARPS][RS_RADIX];
+    __shared__ uint32_t s_goff[RS_RADIX];
+    __shared__ uint32_t s_tstart[RS_RADIX];
+    __shared__ uint32_t s_warp[RS_WARPS + 1];
+    __shared__ uint32_t s_tile;
+
+    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(tile_ctr, 1u);
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) s_whist[w][tid] = 0;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const size_t base = (size_t)tile * RS_TILE;
+
+    uint32_t key[RS_ITEMS], val[RS_ITEMS], rank[RS_ITEMS];
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < RS_ITEMS; k++) {
+        size_t i = base + (size_t)wid * (32 * RS_ITEMS) + (size_t)k * 32 + lane;
+        bool valid = i < n;
+        key[k] = valid ? __ldg(kin + i) : 0xffffffffu;
+        val[k] = valid ? (vin ? __ldg(vin + i) : (uint32_t)i) : 0u;
+        uint32_t active = __ballot_sync(0xffffffffu, valid);
+        uint32_t r = 0;
+        if (valid) {
+            uint32_t d = (key[k] >> shift) & mask;
+            uint32_t peers = __match_any_sync(active, d);
+            uint32_t leader = __ffs(peers) - 1;
+            uint32_t b = 0;
+            if (lane == leader) {
+                b = s_whist[wid][d];
+                s_whist[wid][d] = b + __popc(peers);
+            }
+            b = __shfl_sync(active, b, leader);
+            r = b + __popc(peers & lt);
+        }
+        rank[k] = r;
+        __syncwarp();
+    }
+    __syncthreads();
+    /* per digit: exclusive over warps, tile count */
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) {
+        uint32_t c = s_whist[w][tid];
+        s_whist[w][tid] = run;
+        run += c;
+    }
+    /* publish this tile's count of digit tid, then look back */
+    uint32_t *mine = status + (size_t)tile * RS_RADIX + tid;
+    uint32_t excl = 0;
+    if (tile == 0) {
+        atomicExch(mine, OS_INC | run);
+    } else {
+        atomicExch(mine, OS_AGG | run);
+        /* look back OS_WINDOW tiles per round trip: add aggregates from the
+         * nearest tile outwards until an inclusive prefix; a tile that has
+         * not published yet ends the round, which resumes there */
+        int k = (int)tile - 1;
+        uint32_t spins = 0;
+        bool found = false;
+        while (!found) {
+            uint32_t v[OS_WINDOW];
+#pragma unroll
+            for (int q = 0; q < OS_WINDOW; q++)
+                v[q] = (k - q >= 0) ? *(volatile const uint32_t *)(status + (size_t)(k - q) * RS_RADIX + tid)
+                                    : OS_INC; /* before tile 0: an empty inclusive prefix */
+            int used = 0;
+            bool stalled = false;
+#pragma unroll
+            for (int q = 0; q < OS_WINDOW; q++) {
+                if (found || stalled) continue;
+                if (v[q] & OS_INC) {
+                    excl += v[q] & OS_CNT;
+                    found = true;
+                } else if (v[q] & OS_AGG) {
+                    excl += v[q] & OS_CNT;
+                    used++;
+                } else {
+                    stalled = true;
+                }
+            }
+            k -= used;
+            if (stalled && ++spins > OS_SPIN_LIMIT) {
+                atomicOr(err, FG_DEV_SORT_TIMEOUT);
+                break;
+            }
+        }
+        atomicExch(mine, OS_INC | (excl + run));
+    }
+    s_goff[tid] = __ldg(bases + tid) + excl;
+    {
+        uint32_t tot;
+        s_tstart[tid] = rs_block_excl(run, s_warp, tot);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < RS_ITEMS; k++) {
+        size_t i = base + (size_t)wid * (32 * RS_ITEMS) + (size_t)k * 32 + lane;
+        if (i < n) {
+            uint32_t d = (key[k] >> shift) & mask;
+            uint32_t p = s_tstart[d] + s_whist[wid][d] + rank[k];
+            s_keys[p] = key[k];
+            s_vals[p] = val[k];
+        }
+    }
+    __syncthreads();
+    const uint32_t tile_n = (n - base) < (size_t)RS_TILE ? (uint32_t)(n - base) : (uint32_t)RS_TILE;
+    for (uint32_t i = tid; i < tile_n; i += RS_THREADS) {
+        uint32_t kk = s_keys[i];
+        uint32_t d = (kk >> shift) & mask;
+        uint32_t g = s_goff[d] + (i - s_tstart[d]);
+        if (g < n) { /* only a wait that gave up leaves g unchecked */
+            kout[g] = kk;
+            vout[g] = s_vals[i];
+        }
+    }
+}
+
+bool onesweep_sort(const uint32_t *keys_in, uint32_t *keys_out, uint32_t *vals_out, uint32_t n, uint32_t bits,
+                   uint32_t digit_bits, const RadixScratch &s, uint32_t *os, uint32_t *err, cudaStream_t st)
+{
+    if (digit_bits < 1) digit_bits = 1;
+    if (digit_bits > 8) digit_bits = 8;
+    const int P = radix_passes(bits, digit_bits);
+    if (P < 1 || P > OS_MAX_PASSES || n == 0 || keys_in == keys_out) return false;
+    const uint32_t T = os_tiles(n);
+    uint32_t *status = os;                                        /* [P][T][256] */
+    uint32_t *counts = os + (size_t)OS_MAX_PASSES * RS_RADIX * T; /* [P][256] */
+    uint32_t *ctr = counts + (size_t)OS_MAX_PASSES * RS_RADIX;    /* [P] */
+    cudaMemsetAsync(status, 0, 4 * ((size_t)P * RS_RADIX * T), st);
+    cudaMemsetAsync(counts, 0, 4 * ((size_t)OS_MAX_PASSES * RS_RADIX + 32), st);
+    k_os_hist<<<grid_for((n + RS_THREADS - 1) / RS_THREADS, 4), RS_THREADS, 0, st>>>(keys_in, n, bits, digit_bits,
+                                                                                     (uint32_t)P, counts);
+    k_os_scan<<<P, RS_THREADS, 0, st>>>(counts);
+    const uint32_t *kin = keys_in;
+    const uint32_t *vin = nullptr;
+    bool to_out = (P % 2 == 1);
+    for (int p = 0; p < P; p++) {
+        const uint32_t shift = (uint32_t)p * digit_bits;
+        const uint32_t b = std::min(digit_bits, bits - shift);
+        const uint32_t mask = (1u << b) - 1u;
+        uint32_t *ko = to_out ? keys_out : s.keys_alt;
+        uint32_t *vo = to_out ? vals_out : s.vals_alt;
+        k_os_pass<<<T, RS_THREADS, 0, st>>>(kin, vin, ko, vo, n, shift, mask, status + (size_t)p * RS_RADIX * T,
+                                            counts + (size_t)p * RS_RADIX, ctr + p, err);
+        kin = ko;
+        vin = vo;
+        to_out = !to_out;
+    }
+    return true;
+}
+
 /* ------------------------------------------------------ ranges + reorder
  * FindCellOffsetOrderinPosVelK / FindCellOffsetOrderingPosK
  * (K_HashGrid.cu:70-197): start[key] at the first index of each key run,

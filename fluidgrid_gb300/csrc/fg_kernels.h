@@ -39,6 +39,14 @@ struct RadixScratch {
 };
 size_t radix_hist_words(uint32_t n);
 int radix_passes(uint32_t bits, uint32_t digit_bits);
+/* One-kernel-per-pass variant (decoupled look-back) for the world's fluid
+ * sort: same result as radix_sort with vals_in = 0..n-1.  os is
+ * onesweep_words(n) words of scratch; err receives FG_DEV_SORT_TIMEOUT if a
+ * bounded wait gives up.  Returns false (and does nothing) when the pass
+ * count exceeds what the scratch holds; the caller then uses radix_sort. */
+size_t onesweep_words(uint32_t n);
+bool onesweep_sort(const uint32_t *keys_in, uint32_t *keys_out, uint32_t *vals_out, uint32_t n, uint32_t bits,
+                   uint32_t digit_bits, const RadixScratch &s, uint32_t *os, uint32_t *err, cudaStream_t st);
 /* Stable ascending sort of (key, value) by the low `bits` bits of the key.
  * vals_in == nullptr means values 0..n-1.  keys_out/vals_out may alias
  * keys_in/vals_in (in-place). */

@@ -73,6 +73,7 @@ struct FgWork {
 /* Device status word written by kernels (never trapped on the device). */
 #define FG_DEV_OK 0u
 #define FG_DEV_NONFINITE 1u
+#define FG_DEV_SORT_TIMEOUT 2u /* a one-pass radix sort gave up waiting on a preceding tile */
 #define FG_DEV_RANGE 2u
 
 #endif

@@ -191,6 +191,10 @@ int fg_world_set_graphs(fg_world *w, int on);
  *                         autotuner tries 16, 32 and 64)
  *   FG_OPT_AUTOTUNE_TILES bit mask of the tunables the autotuner varies:
  *                         1 = CTAs per SM, 2 = radix digit width (default 3)
+ *   FG_OPT_ONE_PASS_SORT  1 = the fluid sort runs one kernel per digit pass
+ *                         (decoupled look-back); 0 = upsweep, scan and
+ *                         downsweep kernels per pass (default).  Same order
+ *                         either way.
  * Kernels 0 and 1 (with either target order) produce bit-identical states;
  * kernel 2 sums the same terms in another order.  No kernel's results depend
  * on CTAs per SM or digit width, and kernel 1's not on the list capacity
@@ -198,7 +202,8 @@ int fg_world_set_graphs(fg_world *w, int on);
 enum {
     FG_OPT_NEIGHBOR_LIST = 1, FG_OPT_TARGET_ORDER = 2, FG_OPT_ORDER_PERIOD = 3, FG_OPT_DIGIT_BITS = 4,
     FG_OPT_KERNEL = 5, FG_OPT_AUTOTUNE_PERIOD = 6, FG_OPT_AUTOTUNE_KERNELS = 7, FG_OPT_LIST_CAP = 8,
-    FG_OPT_CTAS_PER_SM = 10, FG_OPT_AUTOTUNE_TILES = 11, FG_OPT_LIST_AUTOGROW = 12, FG_OPT_GRAPH_STEPS = 13
+    FG_OPT_CTAS_PER_SM = 10, FG_OPT_AUTOTUNE_TILES = 11, FG_OPT_LIST_AUTOGROW = 12, FG_OPT_GRAPH_STEPS = 13,
+    FG_OPT_ONE_PASS_SORT = 14
 };
 #define FG_NUM_KERNELS 3
 int fg_world_set_option(fg_world *w, int option, int value);
