@@ -962,7 +962,7 @@ int World::tune_finish()
     return FG_OK;
 }
 
-/* Every FG_LIST_CHECK_PERIOD steps (kernel 3): grow the neighbour-list
+/* Every FG_LIST_CHECK_PERIOD steps (kernel 1): grow the neighbour-list
  * capacity to 1.125x the largest in-range count seen since the last check,
  * so the force pass walks lists instead of buckets as a scene compresses. */
 int World::check_list_cap()

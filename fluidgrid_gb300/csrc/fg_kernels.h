@@ -18,7 +18,7 @@ struct Launch {
     uint32_t nwork;        /* work items */
     uint32_t n;            /* particles (single-scene mode) */
     cudaStream_t stream;
-    uint32_t ctas_per_sm;  /* density/force grids: CTAs per SM (0 = 16) */
+    uint32_t ctas_per_sm;  /* density/force grids: CTAs per SM (0 = 64) */
 };
 
 int sm_count();
