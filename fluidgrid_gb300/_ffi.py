@@ -117,7 +117,7 @@ C_ABI_SYMBOLS = [
     "fg_world_buffer", "fg_world_set_stages", "fg_world_set_fused_integrate", "fg_world_set_sort_digit_bits",
     "fg_world_set_graphs", "fg_world_launches_per_step", "fg_world_stage_profile", "fg_world_timed_steps",
     "fg_world_e2e_steps", "fg_host_alloc", "fg_host_free", "fg_set_device", "fg_probe_fp32_peak",
-    "fg_sort_pairs_noalloc", "fg_world_set_option", "fg_world_get_option", "fg_world_tuning_stats",
+    "fg_sort_pairs_noalloc", "fg_selftest_bounded_wait", "fg_world_set_option", "fg_world_get_option", "fg_world_tuning_stats",
     "fg_world_counters", "fg_world_list_overflows", "fg_world_timed_blocks", "fg_world_diagnostics", "fg_server_config_defaults", "fg_server_create",
     "fg_server_destroy", "fg_server_submit", "fg_server_step", "fg_server_request", "fg_server_result",
     "fg_server_stats",
@@ -182,6 +182,7 @@ def load():
     L.fg_set_device.argtypes = [ctypes.c_int]
     L.fg_probe_fp32_peak.argtypes = [P(c_f)]
     L.fg_sort_pairs_noalloc.argtypes = [VP, VP, c_u32, c_u32, VP]
+    L.fg_selftest_bounded_wait.argtypes = [c_u32, P(c_u32)]
     L.fg_world_set_option.argtypes = [VP, ctypes.c_int, ctypes.c_int]
     L.fg_world_get_option.argtypes = [VP, ctypes.c_int, P(ctypes.c_int)]
     L.fg_world_tuning_stats.argtypes = [VP, P(c_u32), P(c_f)]

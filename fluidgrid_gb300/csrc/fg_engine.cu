@@ -1739,6 +1739,17 @@ int fg_probe_fp32_peak(float *tflops)
 
 const char *fg_last_error(void) { return fg::g_err.c_str(); }
 
+int fg_selftest_bounded_wait(unsigned int spin_limit, unsigned int *flags)
+{
+    if (!flags) return FG_E_INVALID;
+    *flags = 0;
+    if (fg::bounded_wait_selftest(spin_limit, flags) != 0) {
+        fg::set_error("fg_selftest_bounded_wait", cudaGetLastError());
+        return FG_E_CUDA;
+    }
+    return FG_OK;
+}
+
 const char *fg_version(void) { return "fluidgrid_gb300 0.1 sm_103a"; }
 
 } /* extern "C" */

@@ -422,7 +422,8 @@ __global__ void __launch_bounds__(RS_THREADS) k_os_pass(const uint32_t *__restri
                                                        uint32_t n, uint32_t shift, uint32_t mask,
                                                        uint32_t *__restrict__ status,
                                                        const uint32_t *__restrict__ bases,
-                                                       uint32_t *__restrict__ tile_ctr, uint32_t *__restrict__ err)
+                                                       uint32_t *__restrict__ tile_ctr, uint32_t *__restrict__ err,
+                                                       uint32_t spin_limit)
 {
     __shared__ uint32_t s_keys[RS_TILE];
     __shared__ uint32_t s_vals[RS_TILE];
@@ -509,7 +510,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_os_pass(const uint32_t *__restri
                 }
             }
             k -= used;
-            if (stalled && ++spins > OS_SPIN_LIMIT) {
+            if (stalled && ++spins > spin_limit) {
                 atomicOr(err, FG_DEV_SORT_TIMEOUT);
                 break;
             }
@@ -571,12 +572,34 @@ bool onesweep_sort(const uint32_t *keys_in, uint32_t *keys_out, uint32_t *vals_o
         uint32_t *ko = to_out ? keys_out : s.keys_alt;
         uint32_t *vo = to_out ? vals_out : s.vals_alt;
         k_os_pass<<<T, RS_THREADS, 0, st>>>(kin, vin, ko, vo, n, shift, mask, status + (size_t)p * RS_RADIX * T,
-                                            counts + (size_t)p * RS_RADIX, ctr + p, err);
+                                            counts + (size_t)p * RS_RADIX, ctr + p, err, OS_SPIN_LIMIT);
         kin = ko;
         vin = vo;
         to_out = !to_out;
     }
     return true;
+}
+
+/* Self-test of the look-back's bounded wait: one CTA takes tile 1 of a
+ * two-tile sort whose tile 0 never publishes, waits spin_limit rounds, sets
+ * FG_DEV_SORT_TIMEOUT and returns; every access stays inside the buffers
+ * (the scatter skips the positions a wait that gave up leaves unchecked). */
+int bounded_wait_selftest(uint32_t spin_limit, uint32_t *flags)
+{
+    const uint32_t n = 2 * RS_TILE;
+    uint32_t *buf = nullptr;
+    const size_t words = 3 * (size_t)n + 2 * RS_RADIX + RS_RADIX + 2;
+    if (cudaMalloc(&buf, 4 * words) != cudaSuccess) return -1;
+    uint32_t *keys = buf, *kout = buf + n, *vout = buf + 2 * n;
+    uint32_t *status = buf + 3 * (size_t)n, *bases = status + 2 * RS_RADIX, *ctr = bases + RS_RADIX, *err = ctr + 1;
+    cudaMemset(buf, 0, 4 * words);
+    const uint32_t one = 1; /* the only CTA takes tile 1 */
+    cudaMemcpy(ctr, &one, 4, cudaMemcpyHostToDevice);
+    k_os_pass<<<1, RS_THREADS>>>(keys, nullptr, kout, vout, n, 0, 0xffu, status, bases, ctr, err, spin_limit);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(flags, err, 4, cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    return e == cudaSuccess ? 0 : -1;
 }
 
 /* ------------------------------------------------------ ranges + reorder

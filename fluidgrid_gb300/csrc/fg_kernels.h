@@ -45,6 +45,7 @@ int radix_passes(uint32_t bits, uint32_t digit_bits);
  * bounded wait gives up.  Returns false (and does nothing) when the pass
  * count exceeds what the scratch holds; the caller then uses radix_sort. */
 size_t onesweep_words(uint32_t n);
+int bounded_wait_selftest(uint32_t spin_limit, uint32_t *flags);
 bool onesweep_sort(const uint32_t *keys_in, uint32_t *keys_out, uint32_t *vals_out, uint32_t n, uint32_t bits,
                    uint32_t digit_bits, const RadixScratch &s, uint32_t *os, uint32_t *err, cudaStream_t st);
 /* Stable ascending sort of (key, value) by the low `bits` bits of the key.

@@ -275,6 +275,12 @@ int fg_probe_fp32_peak(float *tflops);
 int fg_sort_pairs_noalloc(unsigned int *keys, unsigned int *values, unsigned int keyBits, unsigned int n,
                           fg_stream_t stream);
 
+/* Self-test of the bounded waits in the one-pass sort's look-back: runs one
+ * tile whose predecessor never publishes, so its wait gives up after
+ * spin_limit rounds; *flags receives the device status bits it set (2 = the
+ * sort's wait gave up).  The context stays usable afterwards. */
+int fg_selftest_bounded_wait(unsigned int spin_limit, unsigned int *flags);
+
 /* ---- served form: continuous batching of scenes (no reference
  * counterpart; each scene's step is HeterogeneousSimulator::doTimeStep) ----
  * Requests -- a scene and a step count -- queue on the host.  Every

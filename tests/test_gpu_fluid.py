@@ -477,3 +477,20 @@ def test_one_pass_sort_large_against_numpy():
     order = np.argsort(ku, kind="stable")
     assert np.array_equal(ids, order.astype(np.uint32))
     assert np.array_equal(ks, ku[order])
+
+
+def test_sort_lookback_wait_is_bounded():
+    """The one-pass sort's look-back waits are bounded: a tile whose
+    predecessor never publishes gives up after the given number of rounds,
+    sets the timeout bit (2) that fg_world_sync reports as FG_E_TIMEOUT, and
+    the GPU context stays usable."""
+    import ctypes
+    from fluidgrid_gb300 import _ffi
+    L = _ffi.load()
+    flags = ctypes.c_uint32(0)
+    _ffi.check(L.fg_selftest_bounded_wait(1 << 16, ctypes.byref(flags)), "fg_selftest_bounded_wait")
+    assert flags.value == 2
+    w = World([VARIANTS["ragged_129"]])
+    w.step(2)
+    w.check_finite()
+    w.close()
