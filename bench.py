@@ -145,16 +145,21 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(kernel):
-    """DRAM bytes per particle of `kernel` from the committed ncu summary
-    (lines `traffic_bytes_per_particle <kernel> <value>`), or None."""
+def profile_value(key, kernel):
+    """A figure of `kernel` from the committed ncu summaries (lines
+    `<key> <kernel> <value>` in profiles/*.txt), or None."""
     for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.txt"))):
         with open(path) as f:
             for ln in f:
                 t = ln.split()
-                if len(t) == 3 and t[0] == "traffic_bytes_per_particle" and t[1] == kernel:
+                if len(t) == 3 and t[0] == key and t[1] == kernel:
                     return float(t[2])
     return None
+
+
+def profile_traffic(kernel):
+    """DRAM bytes per particle of `kernel` (ncu, dense phase), or None."""
+    return profile_value("traffic_bytes_per_particle", kernel)
 
 
 def make_scene(name):
@@ -390,7 +395,8 @@ def run_ours(args, rank, world, local):
         dom = max(("forces", "density"), key=lambda k: stages.get(k, 0.0))
         per_p = BYTES_FORCES if dom == "forces" else BYTES_DENSITY
         achieved = per_p * n / (stages[dom] * 1e-3) / 1e9
-        tpp = profile_traffic("k_forces" if dom == "forces" else "k_density")
+        dom_kernel = "k_forces" if dom == "forces" else "k_density"
+        tpp = profile_traffic(dom_kernel)
         cpu = None if args.no_cpu_baseline else cpu_baseline(spec)
         fp32_peak = fp32_peak_tflops()
         pairs_per_step = pair_visits / max(counted, 1)
@@ -413,9 +419,10 @@ def run_ours(args, rank, world, local):
             "latency_ms": {"p50": float(np.percentile(ms_sorted, 50)), "p99": float(np.percentile(ms_sorted, 99)),
                            "max": float(ms_sorted[-1]), "slowest_steps": [int(W + k) for k in np.argsort(-ms)[:5]]},
             "stages_ms": stages,
-            "roofline": {"bound": "hbm", "kernel": "k_forces" if dom == "forces" else "k_density",
+            "roofline": {"bound": "hbm", "kernel": dom_kernel,
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": (tpp * n) if tpp else None, "peak_kind": peak_kind,
+                         "issue_active_pct": profile_value("issue_active_pct", dom_kernel),
                          "bytes_per_particle": per_p, "fp32": fp32},
             "cpu_baseline": ({k: v for k, v in cpu.items() if k != "pairs_per_step"} if cpu else None),
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 32 * n,
