@@ -246,6 +246,12 @@ void gSPHCalculateForcesWithSRB(float4 *oldPositions, float4 *oldVelocity, float
     (void)forces;
     if (!g_have_params || !g_have_kc) { g_status = FG_E_STATE; return; }
     if (!numParticles) { g_status = FG_OK; return; }
+    /* search half-widths of 0..8 cells per axis, as for world scenes */
+    if (_in_cell_size_relation.x < 0 || _in_cell_size_relation.x > 8 || _in_cell_size_relation.y < 0 ||
+        _in_cell_size_relation.y > 8 || _in_cell_size_relation.z < 0 || _in_cell_size_relation.z > 8) {
+        g_status = FG_E_INVALID;
+        return;
+    }
     FgScene S = fluid_scene();
     S.fluid_radius = _in_sph_particle_radius;
     S.rb_radius = _in_srb_particle_radius;
