@@ -807,7 +807,8 @@ uint64_t World::graph_signature() const
 {
     return (uint64_t)((stages & 0xffu) | (fused_integrate ? 0x100u : 0u) | (digit_bits << 9) |
                       (use_list ? 0x10000u : 0u) | ((use_order && order_valid) ? 0x20000u : 0u) |
-                      (use_cc ? 0x40000u : 0u) | ((ctas_per_sm & 0x7fu) << 20)) |
+                      (use_cc ? 0x40000u : 0u) | ((ctas_per_sm & 0x7fu) << 20) |
+                      (one_pass_sort ? 0x8000000u : 0u)) |
            ((uint64_t)nbr.stride << 32);
 }
 
@@ -899,10 +900,11 @@ int World::graph_for_current(cudaGraphExec_t *out, uint32_t nsteps)
  * step() calls. */
 void World::tune_begin()
 {
-    int dims[3], nd = 0;
+    int dims[4], nd = 0;
     if (__builtin_popcount(tune_kernels & 0x7u) >= 2) dims[nd++] = 0;
     if ((tune_tiles & 1u) && !use_cc) dims[nd++] = 1;
     if (tune_tiles & 2u) dims[nd++] = 2;
+    if (tune_tiles & 4u) dims[nd++] = 3;
     tr.ncand = 0;
     if (!nd) return;
     tr.dim = dims[tune_round++ % (uint32_t)nd];
@@ -913,8 +915,13 @@ void World::tune_begin()
         /* CTAs per SM of the 128-thread density/force grids */
         const int v[3] = {16, 32, 64};
         for (int k = 0; k < 3; k++) tr.cand[tr.ncand++] = v[k];
-    } else {
+    } else if (tr.dim == 2) {
         for (int v = 6; v <= 8; v++) tr.cand[tr.ncand++] = v;
+    } else {
+        /* the sort: three kernels per pass (faster for ~1M keys and more)
+         * or one (faster for small scenes) */
+        tr.cand[tr.ncand++] = 0;
+        tr.cand[tr.ncand++] = 1;
     }
     if (tr.ncand < 2) {
         tr.ncand = 0;
@@ -927,7 +934,8 @@ void World::tune_begin()
                 tr.ncand = 0;
                 return;
             }
-    tr.prev = tr.dim == 0 ? current_kernel() : (tr.dim == 1 ? (int)ctas_per_sm : (int)digit_bits);
+    tr.prev = tr.dim == 0 ? current_kernel()
+                          : (tr.dim == 1 ? (int)ctas_per_sm : (tr.dim == 2 ? (int)digit_bits : (one_pass_sort ? 1 : 0)));
     tr.idx = 0;
     tr.active = true;
 }
@@ -936,7 +944,8 @@ void World::tune_apply(int dim, int v)
 {
     if (dim == 0) set_kernel(v);
     else if (dim == 1) ctas_per_sm = (uint32_t)v;
-    else digit_bits = (uint32_t)v;
+    else if (dim == 2) digit_bits = (uint32_t)v;
+    else one_pass_sort = v != 0;
 }
 
 int World::tune_finish()
@@ -1582,7 +1591,7 @@ int fg_world_set_option(fg_world *w, int option, int value)
         W->ctas_per_sm = (uint32_t)value;
         return FG_OK;
     case FG_OPT_AUTOTUNE_TILES:
-        if (value < 0 || value > 3) return FG_E_INVALID;
+        if (value < 0 || value > 7) return FG_E_INVALID;
         W->tune_tiles = (uint32_t)value;
         return FG_OK;
     default: return FG_E_INVALID;

@@ -127,7 +127,7 @@ struct World {
     uint32_t tune_count[3] = {0, 0, 0}; /* steps run with kernel 0..2 */
     float tune_last_ms[3] = {0.f, 0.f, 0.f};
     uint32_t tune_kernels = 0x2; /* candidate kernels bit mask */
-    uint32_t tune_tiles = 0x3;   /* 1: CTAs per SM, 2: digit width */
+    uint32_t tune_tiles = 0x7;   /* 1: CTAs per SM, 2: digit width, 4: sort variant */
     uint32_t tune_round = 0;
     unsigned long long *overflow_counter = nullptr; /* list overflows since the last reset */
     uint32_t *max_count = nullptr; /* largest list count since the last capacity check */

@@ -143,7 +143,8 @@ class World:
         check(self.L.fg_world_tuning_stats(self.h, cnt, ms), "fg_world_tuning_stats")
         return {"steps_per_kernel": list(cnt), "last_trial_ms": [round(x, 4) for x in ms],
                 "kernel": self.get_option("kernel"), "ctas_per_sm": self.get_option("ctas_per_sm"),
-                "digit_bits": self.get_option("digit_bits"), "list_cap": self.get_option("list_cap")}
+                "digit_bits": self.get_option("digit_bits"), "one_pass_sort": self.get_option("one_pass_sort"),
+                "list_cap": self.get_option("list_cap")}
 
     def launches_per_step(self):
         return int(self.L.fg_world_launches_per_step(self.h))

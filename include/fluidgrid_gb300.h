@@ -190,7 +190,8 @@ int fg_world_set_graphs(fg_world *w, int on);
  *                         128-thread density/force grids (0 = 64; the
  *                         autotuner tries 16, 32 and 64)
  *   FG_OPT_AUTOTUNE_TILES bit mask of the tunables the autotuner varies:
- *                         1 = CTAs per SM, 2 = radix digit width (default 3)
+ *                         1 = CTAs per SM, 2 = radix digit width, 4 = the
+ *                         sort variant of FG_OPT_ONE_PASS_SORT (default 7)
  *   FG_OPT_ONE_PASS_SORT  1 = the fluid sort runs one kernel per digit pass
  *                         (decoupled look-back); 0 = upsweep, scan and
  *                         downsweep kernels per pass (default).  Same order
