@@ -679,6 +679,9 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
     if (cur_io && iob) {
         CK0(cudaEventRecord(ev_io_fork, stream));
         CK0(cudaStreamWaitEvent(stream3, ev_io_fork, 0));
+        /* the previous step's velocities go down while this step's
+         * positions come up (the link carries both directions at once) */
+        if (cur_io->prev_vel) CK0(cudaMemcpyAsync(cur_io->ov, vel, iob, cudaMemcpyDeviceToHost, stream3));
         CK0(cudaMemcpyAsync(vel, cur_io->hv, iob, cudaMemcpyHostToDevice, stream3));
         CK0(cudaEventRecord(ev_vel_in, stream3));
         CK0(cudaMemcpyAsync(pos, cur_io->hp, iob, cudaMemcpyHostToDevice, stream));
@@ -786,7 +789,7 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
     }
     if (cur_io && iob) {
         CK0(cudaMemcpyAsync(cur_io->op, pos, iob, cudaMemcpyDeviceToHost, stream));
-        CK0(cudaMemcpyAsync(cur_io->ov, vel, iob, cudaMemcpyDeviceToHost, stream));
+        if (!cur_io->defer_vel) CK0(cudaMemcpyAsync(cur_io->ov, vel, iob, cudaMemcpyDeviceToHost, stream));
     }
     return launches;
 }
@@ -1232,15 +1235,19 @@ int World::e2e_steps(uint32_t nsteps, const float *hp, const float *hv, float *o
     io.op = op;
     io.ov = ov;
     /* pinned buffers: the copies belong to the step (captured with it, the
-     * velocity upload beside the hash and sort); pageable ones are copied
-     * around it */
+     * velocity upload beside the hash and sort, and each step's velocity
+     * download carried into the next step beside its position upload; the
+     * last one follows the last step); pageable ones are copied around it */
     const bool pinned = is_pinned(hp) && is_pinned(hv) && is_pinned(op) && is_pinned(ov);
     const size_t b = 16 * (size_t)n;
     for (uint32_t k = 0; k < nsteps; k++) {
         CK(cudaEventRecord(E.ev[2 * k], stream));
         if (pinned) {
+            io.prev_vel = k > 0;
+            io.defer_vel = true;
             int r = step(1, &io);
             if (r != FG_OK) return r;
+            if (k + 1 == nsteps && b) CK(cudaMemcpyAsync(ov, vel, b, cudaMemcpyDeviceToHost, stream));
         } else {
             if (b) {
                 CK(cudaMemcpyAsync(pos, hp, b, cudaMemcpyHostToDevice, stream));

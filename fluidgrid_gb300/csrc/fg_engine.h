@@ -102,7 +102,16 @@ struct World {
     struct StepIO {
         const void *hp = nullptr, *hv = nullptr;
         void *op = nullptr, *ov = nullptr;
-        bool operator==(const StepIO &o) const { return hp == o.hp && hv == o.hv && op == o.op && ov == o.ov; }
+        /* prev_vel: the step first downloads the previous step's velocities
+         * (still in vel) to ov, beside its own position upload; defer_vel:
+         * the step leaves its velocities for the next step (or the caller)
+         * to download */
+        bool prev_vel = false, defer_vel = false;
+        bool operator==(const StepIO &o) const
+        {
+            return hp == o.hp && hv == o.hv && op == o.op && ov == o.ov && prev_vel == o.prev_vel &&
+                   defer_vel == o.defer_vel;
+        }
     };
     const StepIO *cur_io = nullptr; /* set while step() runs an end-to-end step */
     struct CachedGraph {
