@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(FG_CHUNK, 16) k_density(const FgWork *__restri
             fg_walk27(p.x, p.y, p.z, S, start, end, [&](uint32_t j) {
                 acc.visit<LIST>(__ldg(spos + j), j, px, py, pz, scale, h2, lp, cap);
             });
-            if (LIST) acc.flush(lp, cap);
+            if (LIST) acc.flush(lp, cap, i);
             const float mass = use_o ? mass_o : S->mass;
             const float gas = use_o ? gas_o : S->gas;
             const float rest = use_o ? rest_o : S->rest;
@@ -178,22 +178,20 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                      * the four 32-byte records in flight, one 256-bit load
                      * each */
                     const uint32_t *nl = list.idx + (size_t)tpos * list.stride;
-                    uint4 qn = c ? __ldg(reinterpret_cast<const uint4 *>(nl)) : make_uint4(0u, 0u, 0u, 0u);
-                    for (uint32_t k = 0; k < c; k += 4) {
+                    /* the list is padded with i to whole groups of four */
+                    const uint32_t c4 = (c + 3u) & ~3u;
+                    uint4 qn = c4 ? __ldg(reinterpret_cast<const uint4 *>(nl)) : make_uint4(0u, 0u, 0u, 0u);
+                    for (uint32_t k = 0; k < c4; k += 4) {
                         /* the next four indices load while these records do */
                         const uint4 q = qn;
-                        if (k + 4u < c) qn = __ldg(reinterpret_cast<const uint4 *>(nl + k + 4u));
+                        if (k + 4u < c4) qn = __ldg(reinterpret_cast<const uint4 *>(nl + k + 4u));
                         const uint32_t jj[4] = {q.x, q.y, q.z, q.w};
-                        const uint32_t m = min(4u, c - k);
                         float4 a[4], b[4];
 #pragma unroll
-                        for (int e = 0; e < 4; e++) {
-                            const uint32_t j = (uint32_t)e < m ? jj[e] : jj[0];
-                            fg_ld_rec(list.rec + 2 * j, a[e], b[e]);
-                        }
+                        for (int e = 0; e < 4; e++) fg_ld_rec(list.rec + 2 * jj[e], a[e], b[e]);
 #pragma unroll
                         for (int e = 0; e < 4; e++) {
-                            if ((uint32_t)e < m && jj[e] != i) {
+                            if (jj[e] != i) {
                                 const float dx = fmaf(-a[e].x, scale, px), dy = fmaf(-a[e].y, scale, py),
                                             dz = fmaf(-a[e].z, scale, pz);
                                 const float r2 = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));

@@ -87,10 +87,21 @@ struct DensityAcc {
         }
     }
 
-    /* store an odd last entry (q3), zero-padded to 8 bytes */
-    __device__ __forceinline__ void flush(uint32_t *lp, uint32_t cap) const
+    /* store an odd last entry (q3) and pad the list to a whole group of
+     * four with the target's own index, which the force pass skips, so it
+     * reads only whole groups */
+    __device__ __forceinline__ void flush(uint32_t *lp, uint32_t cap, uint32_t self) const
     {
-        if ((cnt & 1u) && cnt < cap) *reinterpret_cast<uint2 *>(lp + cnt - 1u) = make_uint2(q3, 0u);
+        if (cnt > cap) return;
+        const uint32_t r = cnt & 3u;
+        if (r == 1u) {
+            *reinterpret_cast<uint2 *>(lp + cnt - 1u) = make_uint2(q3, self);
+            *reinterpret_cast<uint2 *>(lp + cnt + 1u) = make_uint2(self, self);
+        } else if (r == 2u) {
+            *reinterpret_cast<uint2 *>(lp + cnt) = make_uint2(self, self);
+        } else if (r == 3u) {
+            *reinterpret_cast<uint2 *>(lp + cnt - 1u) = make_uint2(q3, self);
+        }
     }
 };
 
