@@ -428,7 +428,7 @@ def run_ours(args, rank, world, local):
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 32 * n,
                     "d2h_bytes_per_step": 32 * n, "ms_per_step": e2e_ms / K,
                     "step_ms": {"p50": float(np.percentile(ems, 50)), "p99": float(np.percentile(ems, 99)),
-                                "max": float(ems.max())}},
+                                "max": float(ems.max()), "slowest_steps": [int(W + k) for k in np.argsort(-ems)[:5]]}},
             "gpu_launches": launches * K + K,
             "clocks": clk,
             "forms": forms,

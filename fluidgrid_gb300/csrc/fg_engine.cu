@@ -830,9 +830,8 @@ int World::set_list_cap(uint32_t slots)
         CK(cudaStreamSynchronize(stream));
         const size_t N = std::max<uint64_t>(cap.particles, 1);
         uint32_t *p = nullptr;
-        /* not cleared: every step writes entries [0, cnt) before the force
-         * pass reads them, and the entries past cnt in a 16-byte group it
-         * loads are never used */
+        /* not cleared: every step writes entries [0, cnt rounded up to 4)
+         * before the force pass reads them */
         CK(cudaMalloc(&p, 4 * (size_t)stride * N));
         for (auto &a : allocs)
             if (a == (void *)nbr.idx) a = p;
