@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(FG_CHUNK) k_hash(const FgWork *__restrict__ wo
 void launch_hash(const Launch &L, const float4 *pos, uint32_t *keys, uint32_t *ids)
 {
     if (!L.nwork) return;
-    k_hash<<<grid_for(L.nwork, 16), FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, pos, keys,
+    k_hash<<<grid_for(L.nwork, 64), FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, pos, keys,
                                                              ids);
 }
 
@@ -647,7 +647,7 @@ void launch_cell_ranges(const uint32_t *keys, const uint32_t *ids, const float4 
                         uint32_t *inv, uint32_t *runs, uint32_t *nruns)
 {
     if (!n) return;
-    k_cell_ranges<<<grid_for((n + 255) / 256, 8), 256, 0, st>>>(keys, ids, pos, vel, start, end, spos, svel, n,
+    k_cell_ranges<<<grid_for((n + 255) / 256, 32), 256, 0, st>>>(keys, ids, pos, vel, start, end, spos, svel, n,
                                                                 inv, runs, nruns);
 }
 
