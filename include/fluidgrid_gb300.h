@@ -252,8 +252,12 @@ int fg_world_diagnostics(fg_world *w, double *out);
 int fg_world_timed_blocks(fg_world *w, uint32_t nblocks, uint32_t steps_per_block, size_t flush_bytes, float *ms);
 /* End to end through host memory: per step, copy positions and velocities
  * from host_pos4/host_vel4 to the device, step, copy them back to
- * out_pos4/out_vel4; ms[k] = device time of step k including both copies.
- * Pinned host buffers (fg_host_alloc) keep the copies asynchronous. */
+ * out_pos4/out_vel4 (in and out may be the same buffers); ms[k] = device
+ * time of step k including its copies.  With pinned host buffers
+ * (fg_host_alloc) the copies run inside the step's graph: the velocity
+ * upload beside the hash and sort, and each step's velocity download beside
+ * the next step's position upload (the last one at the end of the call).
+ * Every output has landed when the call returns. */
 int fg_world_e2e_steps(fg_world *w, uint32_t nsteps, const float *host_pos4, const float *host_vel4,
                        float *out_pos4, float *out_vel4, float *ms);
 void *fg_host_alloc(size_t bytes); /* pinned host memory, NULL on failure */
