@@ -12,8 +12,9 @@
  * (z-y-x order, same hashed buckets, a bucket reached twice is summed twice);
  * bucket indices are bit-exact.  Pair arithmetic is reorganised for the
  * GPU: squared-distance tests, rsqrt/rcp instead of divides, compensated
- * (Kahan) density sums; the results agree with the reference arithmetic to
- * the tolerances the parity tests state.
+ * density sums (plain within a bucket, Kahan across buckets); the results
+ * agree with the reference arithmetic to the tolerances the parity tests
+ * state.
  *
  * One thread per particle in sorted order: neighbouring lanes share cells,
  * so neighbour loads broadcast from L1 and sorted float4 loads coalesce.
@@ -71,9 +72,10 @@ __global__ void __launch_bounds__(FG_CHUNK, 16) k_density(const FgWork *__restri
         if (active) {
             const float scale = S->scale, h2 = S->h2;
             const float px = p.x * scale, py = p.y * scale, pz = p.z * scale;
-            fg_walk27(p.x, p.y, p.z, S, start, end, [&](uint32_t j) {
-                acc.visit<LIST>(__ldg(spos + j), j, px, py, pz, scale, h2, lp, cap);
-            });
+            fg_walk27(
+                p.x, p.y, p.z, S, start, end,
+                [&](uint32_t j) { acc.visit<LIST>(__ldg(spos + j), j, px, py, pz, scale, h2, lp, cap); },
+                [&] { acc.end_bucket(); });
             if (LIST) acc.flush(lp, cap, i);
             const float mass = use_o ? mass_o : S->mass;
             const float gas = use_o ? gas_o : S->gas;

@@ -15,10 +15,10 @@ namespace fg {
  * the per-axis hashes selected from registers keeps the code compact (an
  * unrolled walk multiplies the body 27 times and thrashes the instruction
  * cache) and uses no local memory. */
-template <typename Fn>
+template <typename Fn, typename End>
 __device__ __forceinline__ void fg_walk27(float px, float py, float pz, const FgScene *S,
                                           const uint32_t *__restrict__ start, const uint32_t *__restrict__ end,
-                                          Fn &&fn)
+                                          Fn &&fn, End &&bucket_end)
 {
     uint32_t hx[3], hy[3], hz[3];
     fg_neighbour_hashes(px, py, pz, S->cell, hx, hy, hz);
@@ -40,28 +40,51 @@ __device__ __forceinline__ void fg_walk27(float px, float py, float pz, const Fg
             const uint32_t en = fg_sel3(e0, e1, e2, x);
 #pragma unroll 2
             for (uint32_t j = st; j < en; j++) fn(j);
+            bucket_end();
         }
     }
 }
 
-/* One target's state in a density pass: the Kahan sum of (h^2 - l^2)^3 over
- * the candidates with l <= h (an exact 0 at l = h, so the sum equals the
+/* The same walk with nothing to do at the end of a bucket. */
+template <typename Fn>
+__device__ __forceinline__ void fg_walk27(float px, float py, float pz, const FgScene *S,
+                                          const uint32_t *__restrict__ start, const uint32_t *__restrict__ end,
+                                          Fn &&fn)
+{
+    fg_walk27(px, py, pz, S, start, end, fn, [] {});
+}
+
+/* One target's state in a density pass: the sum of (h^2 - l^2)^3 over the
+ * candidates with l <= h (an exact 0 at l = h, so the sum equals the
  * reference's l < h sum) and the force pass's neighbour list (every visit
  * with l <= h, the target's own entries included: testing j != i in the
  * force pass, which waits on memory, is cheaper than in this issue-bound
- * branch), stored two entries (8 bytes) at a time.  Every operation is
- * rounded on its own, so any kernel that visits the same candidates in the
- * same order produces the same bits. */
+ * branch), stored two entries (8 bytes) at a time.  The terms of one bucket
+ * (a few in range) are added plainly; each bucket's partial is then added to
+ * the total with Kahan compensation, which keeps the hot in-range branch to
+ * one addition.  Every operation is rounded on its own, so any kernel that
+ * visits the same candidates in the same order produces the same bits. */
 struct DensityAcc {
-    float s, c;          /* Kahan sum and compensation */
+    float s, c;          /* Kahan sum and compensation over bucket partials */
+    float b;             /* plain sum of the current bucket's terms */
     uint32_t dcnt, cnt;  /* density visits (without a list), list entries */
     uint32_t q2, q3;     /* the last two list entries (q3 the newest) */
 
     __device__ __forceinline__ void init()
     {
-        s = c = 0.0f;
+        s = c = b = 0.0f;
         dcnt = cnt = 0;
         q2 = q3 = 0;
+    }
+
+    /* fold the finished bucket's partial into the compensated total */
+    __device__ __forceinline__ void end_bucket()
+    {
+        const float y = __fsub_rn(b, c);
+        const float u = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(u, s), y);
+        s = u;
+        b = 0.0f;
     }
 
     template <bool LIST>
@@ -72,11 +95,7 @@ struct DensityAcc {
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, __fmul_rn(dz, dz)));
         if (r2 <= h2) {
             const float t = __fsub_rn(h2, r2);
-            const float x = __fmul_rn(__fmul_rn(t, t), t);
-            const float y = __fsub_rn(x, c);
-            const float u = __fadd_rn(s, y);
-            c = __fsub_rn(__fsub_rn(u, s), y);
-            s = u;
+            b = __fadd_rn(b, __fmul_rn(__fmul_rn(t, t), t));
             if (!LIST) dcnt++; /* with a list every visit is an entry: cnt counts them */
             if (LIST) {
                 q2 = q3;
