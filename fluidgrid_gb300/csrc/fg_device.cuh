@@ -153,6 +153,22 @@ __device__ __forceinline__ void fg_wall_friction(float3 &f, float nx, float ny, 
     f.z += s * -tz;
 }
 
+/* Single-instruction approximations (PTX rsqrt.approx.ftz / rcp.approx.ftz)
+ * for operands that are never denormal: a squared pair distance (or 0 for
+ * coincident particles, giving +inf as before) and a density product >= 1. */
+__device__ __forceinline__ float fg_rsqrt_approx(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float fg_rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 __device__ __forceinline__ float3 fg_walls(const FgScene &S, float3 p, float3 v)
 {
     const float eps = 0.00001f;

@@ -254,10 +254,10 @@ __device__ __forceinline__ void fg_pair(float &fx, float &fy, float &fz, float d
                                         float rho_j, float P_j, float4 vj)
 {
     /* every operation rounded on its own: the same bits in every kernel */
-    const float il = rsqrtf(r2);
+    const float il = fg_rsqrt_approx(r2);
     const float l = __fmul_rn(r2, il);
     const float hl = __fsub_rn(h, l);
-    const float irr = __fdividef(1.0f, __fmul_rn(rho_i, rho_j)); /* rho >= 1: no denormal or overflow range */
+    const float irr = fg_rcp_approx(__fmul_rn(rho_i, rho_j)); /* rho >= 1: no denormal or overflow range */
     /* pressure: -(d/l) kSpiky (h-l)^2 (Pi+Pj)/(rho_i rho_j) */
     const float cp = __fmul_rn(__fmul_rn(-__fmul_rn(__fmul_rn(kspiky, hl), hl), __fmul_rn(__fadd_rn(P_i, P_j), irr)),
                                il);
