@@ -167,7 +167,7 @@ def make_scene(name):
     return scenes.WORKLOADS[name]()
 
 
-def cpu_baseline(spec, budget_s=12.0, max_steps=20):
+def cpu_baseline(spec, budget_s=15.0, max_steps=60):
     """The oracle's FP32 restatement of the reference step on all host cores,
     on a bounded sample (whole steps of the same workload until ~budget_s)."""
     from oracle import oracle as O
