@@ -75,6 +75,15 @@ __device__ __forceinline__ void fg_ld_rec(const float4 *p, float4 &a, float4 &b)
         : "l"(p));
 }
 
+/* Eight list entries (one 32-byte sector) in a single 256-bit load of
+ * read-only data; p must be 32-byte aligned. */
+__device__ __forceinline__ void fg_ld_idx8(const uint32_t *p, uint4 &a, uint4 &b)
+{
+    asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w), "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w)
+        : "l"(p));
+}
+
 /* select one of three register values without local-memory indexing */
 __device__ __forceinline__ uint32_t fg_sel3(uint32_t a0, uint32_t a1, uint32_t a2, int k)
 {

@@ -826,7 +826,8 @@ int World::set_list_cap(uint32_t slots)
     slots = (slots + 3u) & ~3u; /* the force pass reads lists four entries at a time */
     if (slots > list_cap_alloc) {
         const uint32_t grown = ((list_cap_alloc + list_cap_alloc / 2u) + 31u) & ~31u;
-        const uint32_t stride = std::max(slots, std::min(grown, FG_LIST_CAP_MAX));
+        /* a multiple of 8: every list starts on a 32-byte boundary */
+        const uint32_t stride = std::max((slots + 7u) & ~7u, std::min(grown, FG_LIST_CAP_MAX));
         CK(cudaStreamSynchronize(stream));
         const size_t N = std::max<uint64_t>(cap.particles, 1);
         uint32_t *p = nullptr;

@@ -176,17 +176,13 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                 const uint32_t c = list.cnt[tpos];
                 if (c <= __ldg(list.cap)) {
                     /* in-range visits in walk order (the target's own
-                     * entries skipped), four indices per 16-byte load, then
-                     * the four 32-byte records in flight, one 256-bit load
-                     * each */
+                     * entries skipped) */
                     const uint32_t *nl = list.idx + (size_t)tpos * list.stride;
                     /* the list is padded with i to whole groups of four */
                     const uint32_t c4 = (c + 3u) & ~3u;
-                    uint4 qn = c4 ? __ldg(reinterpret_cast<const uint4 *>(nl)) : make_uint4(0u, 0u, 0u, 0u);
-                    for (uint32_t k = 0; k < c4; k += 4) {
-                        /* the next four indices load while these records do */
-                        const uint4 q = qn;
-                        if (k + 4u < c4) qn = __ldg(reinterpret_cast<const uint4 *>(nl + k + 4u));
+                    /* four 32-byte records in flight, one 256-bit load each,
+                     * their target's own entries skipped */
+                    auto group = [&](const uint4 q) {
                         const uint32_t jj[4] = {q.x, q.y, q.z, q.w};
                         float4 a[4], b[4];
 #pragma unroll
@@ -201,6 +197,17 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                                         b[e]);
                             }
                         }
+                    };
+                    /* eight indices (one sector, 32-byte aligned: the stride
+                     * is a multiple of 8) per load, the next eight loading
+                     * while these records do */
+                    uint4 qa = make_uint4(0u, 0u, 0u, 0u), qb = qa;
+                    if (c4) fg_ld_idx8(nl, qa, qb);
+                    for (uint32_t k = 0; k < c4; k += 8) {
+                        const uint4 ca = qa, cb = qb;
+                        if (k + 8u < c4) fg_ld_idx8(nl + k + 8u, qa, qb);
+                        group(ca);
+                        if (k + 4u < c4) group(cb);
                     }
                 } else {
                     /* more in-range visits than list slots: walk the buckets */
