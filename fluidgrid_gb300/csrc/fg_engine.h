@@ -15,6 +15,9 @@ namespace fg {
 #define FG_LIST_CAP_DEFAULT 160u
 #define FG_LIST_CAP_MAX 2048u
 #define FG_LIST_CHECK_PERIOD 25u
+/* list strides are multiples of 8 entries: the force pass reads each list
+ * eight entries (one 32-byte sector) at a time from its start */
+static_assert(FG_LIST_CAP_DEFAULT % 8u == 0u && FG_LIST_CAP_MAX % 8u == 0u, "list strides must be multiples of 8");
 
 void set_error(const char *what, cudaError_t e);
 void set_error_msg(const char *what);
