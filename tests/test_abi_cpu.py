@@ -161,3 +161,18 @@ def test_batched_generator():
     assert min(ns) >= 2048 and max(ns) <= 65536
     assert all(len(s.bodies) == (i % 2) for i, s in enumerate(ss))
     assert all(s.bodies[0].local.shape[0] == 512 for s in ss if s.bodies)
+
+
+def _header_enum(prefix):
+    text = open(os.path.join(INC, "fluidgrid_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(%s\w*)\s*=\s*(\d+)" % prefix, text)}
+
+
+def test_option_and_status_codes_match_header():
+    opts = _header_enum("FG_OPT_")
+    assert opts, "no FG_OPT_ enumerators found"
+    assert {"FG_OPT_" + k.upper(): v for k, v in _ffi.OPTIONS.items()} == opts
+    status = _header_enum("FG_E_")
+    status["FG_OK"] = _header_enum("FG_OK")["FG_OK"]
+    assert {v: k for k, v in _ffi.STATUS.items()} == status
