@@ -229,3 +229,101 @@ def test_two_way_coupling_through_reference_launchers(L):
                                   host(bT), q, inv, spec.rb_vlimit)
     for got, want in ((host(tx), x), (host(tv), v), (host(tL), Lr), (host(tqq), qr)):
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def _sphere_grid(L, loc, cm, q, rnb, radius):
+    """gCalcHashKeyWithOffset -> stable sort -> gFindCellOffsetOrderingPos on
+    the GPU (bit-exact against the oracle), as RigidBodySimulator.cpp:146-214
+    builds the static grid and :464-474 the dynamic one."""
+    m = loc.shape[0]
+    rcell = float3(radius, radius, radius)
+    t_loc, t_cm, t_q = dev(loc), dev(cm), dev(q)
+    rkey, rid, rworld, rsorted = u32(m), u32(m), f4(m), f4(m)
+    rstart, rend = u32(rnb), u32(rnb)
+    L.gCalcHashKeyWithOffset(p(rkey), p(rid), p(t_cm), p(t_q), p(t_loc), p(rworld), m, rcell, rnb)
+    rk, ri, rw = O.calc_hash_key_with_offset(loc, cm, q, rnb, (radius,) * 3)
+    assert np.array_equal(host(rkey).view(np.uint32), rk)
+    L.fgc_sort_pairs(p(rkey), p(rid), int(np.ceil(np.log2(rnb))), m)
+    rsk, rsi = O.sort_pairs(rk, ri)
+    assert np.array_equal(host(rid).view(np.uint32), rsi)
+    L.gFindCellOffsetOrderingPos(p(rstart), p(rend), p(rkey), p(rid), p(rworld), p(rsorted), m, rnb)
+    rs0, re0, rsp, _ = O.find_cell_offset(rsk, rsi, rw, None, rnb)
+    T.compare_ranges(host(rstart).view(np.uint32), host(rend).view(np.uint32), rs0, re0)
+    assert np.array_equal(host(rsorted), rsp)
+    return dict(pos=rsorted, start=rstart, end=rend, ref_pos=rsp, ref_start=rs0, ref_end=re0, ids=rsi)
+
+
+def test_static_and_dynamic_grids_through_reference_launchers(L):
+    """SPHCalculateForcesWithSRBK with both the static grid (useStaticRB,
+    K_FluidSim.cu:371-377) and the dynamic grid (:380-386), and
+    CalculateRigidBodyForcesFromRBK (K_RigidBodySim.cu:18-61) with its
+    static-grid term (numSRB > 0), each against the oracle."""
+    spec = R.static_dynamic_scene()
+    n, nb = spec.n, spec.nbuckets
+    L.gInitializeCommonFluidParams(spec.common_params())
+    L.gInitializeKernelParams(kcache(spec.h))
+    vel0 = np.zeros((n, 4), np.float32)
+    vel0[:, :3] = np.random.default_rng(9).normal(0, 0.2, (n, 3))
+    ref = T.oracle_grid(spec, spec.pos, vel0)
+    opos, ovel = dev(ref["spos"]), dev(ref["svel"])
+    start, end = dev(ref["start"].view(np.int32)), dev(ref["end"].view(np.int32))
+    pid = dev(ref["ids"].view(np.int32))
+    key = dev(ref["skeys"].view(np.int32))
+    dp = torch.zeros((n, 2), dtype=torch.float32, device="cuda")
+    L.gCalcMassDensity(p(opos), p(dp), p(key), p(start), p(end), n, spec.gas, spec.rest, spec.mass)
+    rnb = int(np.prod(spec.rb_buckets))
+    r = spec.rb_radius
+    # static grid: body 0's spheres in world space (RigidBodySimulator.cpp:146-214)
+    b0 = spec.bodies[0]
+    sloc = np.c_[b0.local[:, :3], np.zeros(len(b0.local), np.float32)].astype(np.float32)
+    scm = np.array([list(b0.position) + [0.0]], np.float32)
+    sq = np.array([b0.orientation], np.float32)
+    sg = _sphere_grid(L, sloc, scm, sq, rnb, r)
+    # dynamic grid: bodies 1 and 2, w = dynamic body index
+    dyn = spec.bodies[1:]
+    dloc = np.concatenate([np.c_[b.local[:, :3], np.full(len(b.local), i, np.float32)]
+                           for i, b in enumerate(dyn)]).astype(np.float32)
+    dcm = np.array([list(b.position) + [0.0] for b in dyn], np.float32)
+    dq = np.array([b.orientation for b in dyn], np.float32)
+    bvel = np.array([[0.2, -0.1, 0.0, 0.0], [-0.3, 0.05, 0.1, 0.0]], np.float32)
+    dg = _sphere_grid(L, dloc, dcm, dq, rnb, r)
+    t_bv, t_cm = dev(bvel), dev(dcm)
+    rcell = float3(r, r, r)
+    # fluid side: both grids
+    newvel = dev(vel0)
+    L.gSPHCalculateForcesWithSRB(p(opos), p(ovel), p(f4(1)), p(newvel), p(dp), p(pid), p(start), p(end), n,
+                                 spec.mass, spec.visc, spec.fluid_radius, int3(*spec.f2r_rel), r, rcell, spec.ck,
+                                 spec.ckd, p(sg["pos"]), p(sg["start"]), p(sg["end"]), rnb, p(dg["pos"]), p(t_bv),
+                                 p(dg["start"]), p(dg["end"]), rnb, True, True)
+    assert L.fgc_last_status() == 0
+    kc = O.kernels_cache(spec.h)
+    cp = O.contact_params(spec.fluid_radius, r, spec.ck, spec.ckd, (r,) * 3, spec.f2r_rel, 0.003)
+    o_sg = O.contact_grid(sg["ref_pos"], None, sg["ref_start"], sg["ref_end"], rnb)
+    o_dg = O.contact_grid(dg["ref_pos"], bvel, dg["ref_start"], dg["ref_end"], rnb)
+    dpg = host(dp)
+    args = (ref["spos"], ref["svel"], dpg, ref["start"], ref["end"], ref["ids"], spec.mass, spec.visc, ref["p"], kc)
+    nv = O.forces(*args, newvel_init=vel0, contact=(cp, o_sg, o_dg))
+    nv_dyn = O.forces(*args, newvel_init=vel0, contact=(cp, None, o_dg))
+    Fv, Fvr = T.force_from_vel(host(newvel), vel0, spec.dt), T.force_from_vel(nv, vel0, spec.dt)
+    touched = np.linalg.norm(Fvr - T.force_from_vel(nv_dyn, vel0, spec.dt), axis=1) > 0
+    assert touched.sum() > 20, "the static-grid term must act on some fluid particles"
+    mag = np.linalg.norm(Fvr, axis=1)
+    assert (np.linalg.norm(Fv - Fvr, axis=1) / np.maximum(mag, np.median(mag))).max() <= 2e-4
+    # rigid side: dynamic spheres against the other dynamic body and the static grid
+    m = dloc.shape[0]
+    Fo, To = f4(m), f4(m)
+    L.gCalculateRigidBodyForcesFromRB(p(dg["pos"]), p(t_bv), p(t_cm), p(To), p(Fo), p(dg["start"]), p(dg["end"]),
+                                      m, rcell, r, rnb, rnb, p(sg["pos"]), p(sg["start"]), p(sg["end"]),
+                                      spec.rbrb_k, spec.rbrb_kd, 1)
+    assert L.fgc_last_status() == 0
+    srb = (sg["ref_pos"], sg["ref_start"], sg["ref_end"], rnb, 1)
+    Fr, Tr = O.rb_forces_from_rb(dg["ref_pos"], bvel, dcm, dg["ref_start"], dg["ref_end"], (r,) * 3, r, rnb,
+                                 spec.rbrb_k, spec.rbrb_kd, srb=srb)
+    Fd, _ = O.rb_forces_from_rb(dg["ref_pos"], bvel, dcm, dg["ref_start"], dg["ref_end"], (r,) * 3, r, rnb,
+                                spec.rbrb_k, spec.rbrb_kd)
+    n_dyn = int((np.abs(Fd[:, :3]) > 0).any(1).sum())
+    n_sta = int((np.abs(Fr[:, :3] - Fd[:, :3]) > 0).any(1).sum())
+    assert n_dyn > 10 and n_sta > 10, (n_dyn, n_sta)
+    Fg, Tg = host(Fo), host(To)
+    assert R._close(Fg[:, :3], Fr[:, :3], 1e-4) and R._close(Tg[:, :3], Tr[:, :3], 1e-4)
+    assert np.array_equal(Fg[:, 3], Fr[:, 3]) and np.array_equal(Tg[:, 3], Tr[:, 3])

@@ -142,13 +142,90 @@ def test_body_reduction_and_fp64_integration():
         assert np.allclose(g[name], ref, rtol=1e-12, atol=1e-14), name
 
 
-def test_rigid_rigid_contact_runs_and_is_symmetric_in_sum():
-    spec = rigid_scene(nbodies=2, rb_rb=True)
-    spec.bodies[1].position = (0.25 + 0.17, 0.38, 0.37)  # overlap the two bodies
-    w = World([spec])
-    w.step(3)
-    w.check_finite()
-    w.close()
+def static_dynamic_scene():
+    """Three boxes/spheres straddling the fluid surface (y ~ 0.37): body 0 of
+    mass 0 (static: the reference's static rigid-body grid,
+    RigidBodySimulator.cpp:146-214), bodies 1 and 2 dynamic; body 1 overlaps
+    body 0 and body 2.  Rigid/rigid contact on."""
+    spec = rigid_scene(nbodies=1, rb_rb=True)
+    rng = np.random.default_rng(8)
+    ident = (0.0, 0.0, 0.0, 1.0)
+    spec.bodies = [Body(local=box_surface(0.2, 1024, rng), mass=0.0, position=(0.25, 0.38, 0.37),
+                        orientation=ident),
+                   Body(local=box_surface(0.2, 1024, rng), mass=10.0, position=(0.42, 0.40, 0.37),
+                        orientation=ident),
+                   Body(local=sphere_surface(0.12, 700), mass=8.0, position=(0.63, 0.40, 0.39),
+                        orientation=ident)]
+    return spec
+
+
+def test_rigid_rigid_and_static_contact_match_oracle():
+    """One world step of a scene with a static body and two touching dynamic
+    bodies against the oracle from the identical state:
+      - fluid forces with the static-grid term (K_FluidSim.cu:371-377) and the
+        dynamic-grid term (:380-386);
+      - per-sphere force/torque of the dynamic bodies: fluid contact
+        (CalculateRBForcesFromFluidsK) plus sphere/sphere contact with the
+        other dynamic body and with the static grid
+        (CalculateRigidBodyForcesFromRBK, K_RigidBodySim.cu:18-61);
+      - the static body is never moved."""
+    spec = static_dynamic_scene()
+    pos0, v0, before, g = _run(spec)
+    nb_r = int(np.prod(spec.rb_buckets))
+    cell = (spec.rb_radius,) * 3
+    r = spec.rb_radius
+    _, _, world = O.calc_hash_key_with_offset(before["RB_LOCAL"], before["BODY_XF"], before["BODY_QF"], nb_r, cell)
+    body = world[:, 3].astype(np.int64)
+    grids = {}
+    for name, sel in (("static", body == 0), ("dynamic", body > 0)):
+        pts = np.ascontiguousarray(world[sel])
+        keys, ids = O.calc_hash_key(pts, nb_r, cell)
+        sk, si = O.sort_pairs(keys, ids)
+        st, en, sp, _ = O.find_cell_offset(sk, si, pts, None, nb_r)
+        grids[name] = dict(spos=sp, start=st, end=en, ids=si, first=int(np.flatnonzero(sel)[0]))
+    sg, dg = grids["static"], grids["dynamic"]
+    bvel = before["BODY_VF"]
+    assert not bvel[0].any()
+    # fluid side
+    fl = T.oracle_grid(spec, pos0, v0)
+    kc = O.kernels_cache(spec.h)
+    cp = O.contact_params(spec.fluid_radius, r, spec.ck, spec.ckd, cell, spec.f2r_rel, 0.003)
+    o_sg = O.contact_grid(sg["spos"], None, sg["start"], sg["end"], nb_r)
+    o_dg = O.contact_grid(dg["spos"], bvel, dg["start"], dg["end"], nb_r)
+    args = (fl["spos"], fl["svel"], g["DP"], fl["start"], fl["end"], fl["ids"], spec.mass, spec.visc, fl["p"], kc)
+    nv = O.forces(*args, newvel_init=v0, contact=(cp, o_sg, o_dg))
+    nv_dyn = O.forces(*args, newvel_init=v0, contact=(cp, None, o_dg))
+    Fg = T.force_from_vel(g["VEL"], v0, spec.dt)
+    Fr = T.force_from_vel(nv, v0, spec.dt)
+    touched = np.linalg.norm(Fr - T.force_from_vel(nv_dyn, v0, spec.dt), axis=1) > 0
+    assert touched.sum() > 20, "the static body must act on some fluid particles"
+    mag = np.linalg.norm(Fr, axis=1)
+    assert (np.linalg.norm(Fg - Fr, axis=1) / np.maximum(mag, np.median(mag))).max() <= 2e-4
+    # rigid side, dynamic spheres (sorted order of the dynamic grid)
+    Ff, Tf = O.rb_forces_from_fluids(dg["spos"], bvel, before["BODY_XF"], r, fl["spos"], fl["svel"], fl["start"],
+                                     fl["end"], spec.fluid_radius, spec.cell_size, spec.nbuckets, spec.r2f_rel,
+                                     spec.ck, spec.ckd)
+    srb = (sg["spos"], sg["start"], sg["end"], nb_r, 1)
+    Fr_rb, Tr_rb = O.rb_forces_from_rb(dg["spos"], bvel, before["BODY_XF"], dg["start"], dg["end"], cell, r, nb_r,
+                                       spec.rbrb_k, spec.rbrb_kd, srb=srb)
+    Fd, _ = O.rb_forces_from_rb(dg["spos"], bvel, before["BODY_XF"], dg["start"], dg["end"], cell, r, nb_r,
+                                spec.rbrb_k, spec.rbrb_kd)
+    n_dyn = int((np.abs(Fd[:, :3]) > 0).any(1).sum())
+    n_sta = int((np.abs(Fr_rb[:, :3] - Fd[:, :3]) > 0).any(1).sum())
+    assert n_dyn > 10 and n_sta > 10, (n_dyn, n_sta)
+    Fw = (Ff[:, :3] + Fr_rb[:, :3]).astype(np.float32)
+    Tw = (Tf[:, :3] + Tr_rb[:, :3]).astype(np.float32)
+    # the world writes each sphere's result at its unsorted index
+    unsorted = dg["first"] + dg["ids"]
+    assert _close(g["RB_FORCE"][unsorted, :3], Fw, 1e-4)
+    assert _close(g["RB_TORQUE"][unsorted, :3], Tw, 1e-4)
+    assert np.array_equal(g["RB_FORCE"][unsorted, 3], dg["spos"][:, 3])
+    # the static body keeps its pose and zero velocity
+    assert np.array_equal(g["BODY_X"][0].view(np.uint64), before["BODY_X"][0].view(np.uint64))
+    assert np.array_equal(g["BODY_Q"][0].view(np.uint64), before["BODY_Q"][0].view(np.uint64))
+    assert not g["BODY_V"][0].any()
+    # the dynamic bodies move
+    assert not np.array_equal(g["BODY_X"][1:], before["BODY_X"][1:])
 
 
 def test_rigid_world_multi_step_finite():
