@@ -69,7 +69,10 @@ def build_grid(lib, pos4, cell, nb):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference-dir", default="/root/reference")
+    here = os.path.dirname(os.path.abspath(__file__))
+    default = os.environ.get("FLUIDGRID_REFERENCE_DIR") or os.path.join(here, "..", "..", "..", "reference")
+    ap.add_argument("--reference-dir", default=os.path.abspath(default),
+                    help="FluidGrid checkout ($FLUIDGRID_REFERENCE_DIR, else `reference` beside this repository)")
     args = ap.parse_args()
     if not os.path.isdir(os.path.join(args.reference_dir, "GPU_Kernels")):
         print("reference sources not found; nothing generated", file=sys.stderr)
