@@ -12,17 +12,23 @@
  * Limits and rules:
  *  - at most FG_NOALLOC_MAX_PAIRS (1,048,576) pairs per call; larger n is
  *    rejected with FG_E_INVALID and a message in fg_last_error();
- *  - the array (FG_NOALLOC_WORDS 32-bit words, about 8.65 MB) is held on every
- *    GPU that loads this library until the process exits;
+ *  - the array (FG_NOALLOC_WORDS = 2,228,480 32-bit words: 8,913,920 bytes,
+ *    8.91 MB or 8.5 MiB) is held on every GPU that loads this library until
+ *    the process exits;
  *  - all calls share the array, so calls that overlap on the GPU (different
  *    streams, or several host threads) race and corrupt each other's results;
  *    serialise them;
  *  - every scratch word a call reads was written earlier by the same call, so
  *    nothing has to start at zero and the contents left by the previous call
  *    do not matter;
- *  - the first call on a device looks up the array's device address
- *    (cudaGetSymbolAddress with that device current) and caches it; make that
- *    first call before any stream capture. */
+ *  - each call looks up the array's device address (cudaGetSymbolAddress
+ *    with the caller's device current), so a context torn down and created
+ *    again (cudaDeviceReset) is followed; while the stream is being captured
+ *    the address cached by the last uncaptured call on that device is used
+ *    instead, so the first call on a device must come before any stream
+ *    capture;
+ *  - an error left pending by earlier, unrelated work is cleared on entry, so
+ *    FG_E_CUDA reports only this call's own launches and copies. */
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <mutex>
@@ -39,6 +45,7 @@
 #define FG_NOALLOC_WORDS (2u * FG_NOALLOC_MAX_PAIRS + FG_NOALLOC_HIST_WORDS)
 
 static __device__ __align__(256) uint32_t g_noalloc_scratch[FG_NOALLOC_WORDS];
+static_assert(sizeof(g_noalloc_scratch) == 8913920u, "the documented scratch size is 8,913,920 bytes");
 
 namespace {
 
@@ -46,10 +53,12 @@ const int kMaxDevices = 64;
 uint32_t *g_scratch_ptr[kMaxDevices];
 std::mutex g_setup_mu;
 
-/* Device address of g_noalloc_scratch on the current device; looked up once
- * per device.  In host code the symbol's name only stands for the array, it
- * is not a device address. */
-int scratch_for_current_device(uint32_t **out)
+/* Device address of g_noalloc_scratch on the current device.  In host code
+ * the symbol's name only stands for the array, it is not a device address.
+ * Outside stream capture the address is looked up on every call (cheap), so
+ * it follows a context that was reset and created again; while `stream` is
+ * capturing, the address cached by the last uncaptured call is used. */
+int scratch_for_current_device(cudaStream_t stream, uint32_t **out)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -61,8 +70,19 @@ int scratch_for_current_device(uint32_t **out)
         fg::set_error_msg("fg_sort_pairs_noalloc: device ordinal out of range");
         return FG_E_UNSUPPORTED;
     }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(stream, &cs);
+    if (e != cudaSuccess) {
+        fg::set_error("cudaStreamIsCapturing", e);
+        return FG_E_CUDA;
+    }
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (cs != cudaStreamCaptureStatusNone) {
+        if (!g_scratch_ptr[dev]) {
+            fg::set_error_msg("fg_sort_pairs_noalloc: first call on this device made during stream capture");
+            return FG_E_STATE;
+        }
+    } else {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
@@ -91,14 +111,16 @@ extern "C" int fg_sort_pairs_noalloc(unsigned int *keys, unsigned int *values, u
     }
     if (keyBits > 32) keyBits = 32;
     uint32_t *s = nullptr;
-    int r = scratch_for_current_device(&s);
+    int r = scratch_for_current_device((cudaStream_t)stream, &s);
     if (r != FG_OK) return r;
     fg::RadixScratch rs;
     rs.keys_alt = s;
     rs.vals_alt = s + FG_NOALLOC_MAX_PAIRS;
     rs.hist = s + 2u * FG_NOALLOC_MAX_PAIRS;
-    fg::radix_sort(keys, values, keys, values, n, keyBits, 8, rs, (cudaStream_t)stream);
-    cudaError_t e = cudaPeekAtLastError();
+    (void)cudaGetLastError(); /* only this call's own errors are reported below */
+    cudaError_t e = fg::radix_sort(keys, values, keys, values, n, keyBits, 8, rs, (cudaStream_t)stream);
+    const cudaError_t le = cudaGetLastError();
+    if (e == cudaSuccess) e = le;
     if (e != cudaSuccess) {
         fg::set_error("fg_sort_pairs_noalloc", e);
         return FG_E_CUDA;
