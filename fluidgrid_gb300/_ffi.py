@@ -101,6 +101,11 @@ STAGE_HASH, STAGE_SORT, STAGE_RANGES, STAGE_DENSITY = 1, 2, 4, 8
 STAGE_RB_GRID, STAGE_RB_CONTACT, STAGE_FORCES, STAGE_BODIES = 16, 32, 64, 128
 STAGE_ALL = 255
 
+# fg_world_run_stage: one stage of a step at a time, in this order
+RUN = {"neighbourhood": 1, "density": 2, "rb_grid": 3, "rb_from_fluid": 4, "rb_from_rb": 5, "forces": 6,
+       "body_sums": 7, "body_integrate": 8, "integrate": 9}
+RUN_WITH_CONTACT = 1
+
 OPTIONS = {"neighbor_list": 1, "target_order": 2, "order_period": 3, "digit_bits": 4, "kernel": 5,
            "autotune_period": 6, "autotune_kernels": 7, "list_cap": 8, "ctas_per_sm": 10,
            "autotune_tiles": 11, "list_autogrow": 12, "graph_steps": 13, "one_pass_sort": 14}
@@ -111,7 +116,8 @@ STATUS = {0: "FG_OK", 1: "FG_E_INVALID", 2: "FG_E_CUDA", 3: "FG_E_OOM", 4: "FG_E
 
 # every symbol the two public headers declare
 C_ABI_SYMBOLS = [
-    "fg_scene_desc_defaults", "fg_world_create", "fg_world_destroy", "fg_world_step", "fg_world_sync",
+    "fg_scene_desc_defaults", "fg_world_create", "fg_world_destroy", "fg_world_step", "fg_world_run_stage",
+    "fg_world_sync",
     "fg_world_check", "fg_world_upload", "fg_world_download", "fg_world_scene_upload", "fg_world_scene_download",
     "fg_world_particles", "fg_world_scenes", "fg_world_spheres", "fg_world_bodies", "fg_world_scene_layout",
     "fg_world_buffer", "fg_world_set_stages", "fg_world_set_fused_integrate", "fg_world_set_sort_digit_bits",
@@ -157,6 +163,7 @@ def load():
     for n in ("fg_world_destroy", "fg_world_sync", "fg_world_check"):
         getattr(L, n).argtypes = [VP]
     L.fg_world_step.argtypes = [VP, c_u32]
+    L.fg_world_run_stage.argtypes = [VP, ctypes.c_int, ctypes.c_int]
     L.fg_world_upload.argtypes = [VP, VP, VP]
     L.fg_world_download.argtypes = [VP, VP, VP]
     L.fg_world_scene_upload.argtypes = [VP, c_u32, VP, VP]

@@ -1000,6 +1000,10 @@ bool World::host_boundary(uint64_t s) const
 
 int World::step(uint32_t nsteps, const StepIO *io)
 {
+    if (staged_done) {
+        set_error_msg("a stage-by-stage step is in progress: finish it with FG_RUN_INTEGRATE");
+        return FG_E_STATE;
+    }
     cur_io = io;
     int r = step_loop(nsteps);
     cur_io = nullptr;
@@ -1063,6 +1067,171 @@ int World::step_loop(uint32_t nsteps)
         set_error("step", e);
         return FG_E_CUDA;
     }
+    return FG_OK;
+}
+
+/* The stages of one step enqueued one call at a time, in the order of the
+ * reference's two-way step (HeterogeneousSimulator.cpp:57-126 with
+ * RigidBodySimulator.cpp:313-611): neighbourhood (hash, sort, ranges),
+ * density, rigid-sphere grid, sphere forces from the fluid and from other
+ * bodies, fluid forces (velocity only), per-body sums, body integration,
+ * fluid integration.  The kernels are those of a whole step, so a staged
+ * step gives the same bits; no graph is captured and no autotuning round
+ * runs.  A stage whose inputs were not produced earlier in the same step
+ * returns FG_E_STATE. */
+int World::run_stage(int stage, int flags)
+{
+    auto bit = [](int s) { return 1u << s; };
+    auto need = [&](uint32_t mask, const char *msg) {
+        if ((staged_done & mask) == mask) return true;
+        set_error_msg(msg);
+        return false;
+    };
+    const bool rb = nbodies > 0;
+    const Launch L = fluid_launch();
+    switch (stage) {
+    case FG_RUN_NEIGHBOURHOOD: {
+        if (staged_done) {
+            set_error_msg("FG_RUN_NEIGHBOURHOOD: the previous staged step has not reached FG_RUN_INTEGRATE");
+            return FG_E_STATE;
+        }
+        if (tr.active) { /* a staged step is no autotuning trial: keep the value in use */
+            tune_apply(tr.dim, tr.prev);
+            tr.active = false;
+        }
+        if (use_list && list_autogrow && step_count && (step_count % FG_LIST_CHECK_PERIOD == 0)) {
+            int r = check_list_cap();
+            if (r != FG_OK) return r;
+        }
+        if (use_order && !needs_runs() && (!order_valid || (order_period && step_count % order_period == 0)))
+            enqueue_order_refresh();
+        launch_hash(L, pos, keys_u, nullptr);
+        if (!(one_pass_sort && onesweep_sort(keys_u, keys, ids, n, key_bits, digit_bits, rs, os_scratch, status_d,
+                                             stream)))
+            radix_sort(keys_u, nullptr, keys, ids, n, key_bits, digit_bits, rs, stream);
+        cudaMemsetAsync(start, 0xff, 4 * (size_t)total_buckets, stream);
+        if (needs_runs()) {
+            cudaMemsetAsync(nruns, 0, 4, stream);
+            launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv, runs, nruns);
+        } else {
+            launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv);
+        }
+        break;
+    }
+    case FG_RUN_DENSITY:
+        if (!need(bit(FG_RUN_NEIGHBOURHOOD), "FG_RUN_DENSITY needs FG_RUN_NEIGHBOURHOOD first")) return FG_E_STATE;
+        if (use_cc)
+            launch_density_cc(single ? nullptr : scenes_d, &scenes_h[0], nscenes, runs, nruns, keys, spos, svel, start,
+                              end, dp, nbr.rec, n, stream);
+        else
+            launch_density(L, spos, start, end, dp, 0.f, 0.f, 0.f, 0, svel, use_list ? &nbr : nullptr,
+                           target_order(), pair_counter);
+        break;
+    case FG_RUN_RB_GRID: {
+        if (!rb) break;
+        if (staged_done & bit(FG_RUN_BODY_INTEGRATE)) {
+            set_error_msg("FG_RUN_RB_GRID must come before FG_RUN_BODY_INTEGRATE");
+            return FG_E_STATE;
+        }
+        uint32_t launches = 0;
+        const uint32_t keep = stages;
+        stages = FG_STAGE_ALL;
+        enqueue_rb_grid(stream, nullptr, launches);
+        stages = keep;
+        break;
+    }
+    case FG_RUN_RB_FROM_FLUID:
+        if (!rb) break;
+        if (!need(bit(FG_RUN_NEIGHBOURHOOD) | bit(FG_RUN_RB_GRID),
+                  "FG_RUN_RB_FROM_FLUID needs FG_RUN_NEIGHBOURHOOD and FG_RUN_RB_GRID first"))
+            return FG_E_STATE;
+        launch_rb_from_fluid(sphere_launch(), rb_spos, rb_ids, bvf, bxf, spos, svel, start, end, rb_force, rb_torque,
+                             0);
+        break;
+    case FG_RUN_RB_FROM_RB:
+        if (!rb || !any_rb_rb) break;
+        if (!need(bit(FG_RUN_RB_FROM_FLUID), "FG_RUN_RB_FROM_RB adds to FG_RUN_RB_FROM_FLUID: run that first"))
+            return FG_E_STATE;
+        launch_rb_from_rb(sphere_launch(), rb_spos, rb_ids, bvf, bxf, rb_start, rb_end, rb_force, rb_torque, nullptr,
+                          1);
+        break;
+    case FG_RUN_FORCES: {
+        if (!need(bit(FG_RUN_DENSITY), "FG_RUN_FORCES needs FG_RUN_DENSITY first")) return FG_E_STATE;
+        const bool contact = rb && (flags & FG_RUN_WITH_CONTACT);
+        if (contact && !need(bit(FG_RUN_RB_GRID), "FG_RUN_FORCES with contact needs FG_RUN_RB_GRID first"))
+            return FG_E_STATE;
+        if (staged_done & bit(FG_RUN_BODY_INTEGRATE)) {
+            set_error_msg("FG_RUN_FORCES reads the bodies' old velocities: run it before FG_RUN_BODY_INTEGRATE");
+            return FG_E_STATE;
+        }
+        RigidGrid G;
+        G.spos = rb_spos;
+        G.start = rb_start;
+        G.end = rb_end;
+        G.body_vel = bvf;
+        G.aabb = aabb;
+        G.own_geometry = 0;
+        G.nb = 0;
+        G.mask = 0;
+        ForceOut o;
+        o.vel = vel;
+        o.pos = nullptr; /* FG_RUN_INTEGRATE moves the particles */
+        if (use_cc)
+            launch_forces_cc(single ? nullptr : scenes_d, &scenes_h[0], nscenes, runs, nruns, keys, spos, svel,
+                             nbr.rec, start, end, ids, o, contact ? &G : nullptr, n, stream);
+        else
+            launch_forces(L, spos, svel, dp, start, end, ids, o, contact ? &G : nullptr, nullptr, 0.f, 0.f, 0,
+                          use_list ? &nbr : nullptr, target_order());
+        break;
+    }
+    case FG_RUN_BODY_SUMS:
+    case FG_RUN_BODY_INTEGRATE: {
+        if (!rb) break;
+        const uint32_t want = bit(FG_RUN_RB_FROM_FLUID) | (any_rb_rb ? bit(FG_RUN_RB_FROM_RB) : 0u) |
+                              (stage == FG_RUN_BODY_INTEGRATE ? bit(FG_RUN_BODY_SUMS) | bit(FG_RUN_FORCES) : 0u);
+        if (!need(want, stage == FG_RUN_BODY_SUMS
+                            ? "FG_RUN_BODY_SUMS needs the sphere forces (FG_RUN_RB_FROM_FLUID, and FG_RUN_RB_FROM_RB "
+                              "when bodies can touch) first"
+                            : "FG_RUN_BODY_INTEGRATE needs FG_RUN_BODY_SUMS and FG_RUN_FORCES first"))
+            return FG_E_STATE;
+        BodyState b;
+        b.x = bx; b.v = bv; b.q = bq; b.L = bL;
+        b.inv_inertia = binv;
+        b.mass = bmass;
+        b.x_f = bxf; b.v_f = bvf; b.q_f = bqf;
+        b.force_sum = bfs; b.torque_sum = bts;
+        b.partial = body_part;
+        launch_body_update(single ? nullptr : scenes_d, &scenes_h[0], body_scene, body_first, body_count, nbodies,
+                           rb_force, rb_torque, b, stage == FG_RUN_BODY_INTEGRATE ? 1 : 0, stream);
+        break;
+    }
+    case FG_RUN_INTEGRATE: {
+        const uint32_t want = bit(FG_RUN_FORCES) | (rb ? bit(FG_RUN_BODY_INTEGRATE) : 0u);
+        if (!need(want, "FG_RUN_INTEGRATE ends the step: it needs FG_RUN_FORCES (and FG_RUN_BODY_INTEGRATE with "
+                        "bodies) first"))
+            return FG_E_STATE;
+        launch_integrate(L, pos, vel);
+        cudaError_t e = cudaPeekAtLastError();
+        if (e != cudaSuccess) {
+            set_error("staged step", e);
+            return FG_E_CUDA;
+        }
+        tune_count[current_kernel()]++;
+        counted_steps++;
+        step_count++;
+        staged_done = 0;
+        return FG_OK;
+    }
+    default:
+        set_error_msg("unknown stage");
+        return FG_E_INVALID;
+    }
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess) {
+        set_error("staged step", e);
+        return FG_E_CUDA;
+    }
+    staged_done |= bit(stage);
     return FG_OK;
 }
 
@@ -1407,6 +1576,12 @@ int fg_world_step(fg_world *w, uint32_t nsteps)
 {
     if (!w) return FG_E_INVALID;
     return ((World *)w)->step(nsteps);
+}
+
+int fg_world_run_stage(fg_world *w, int stage, int flags)
+{
+    if (!w) return FG_E_INVALID;
+    return ((World *)w)->run_stage(stage, flags);
 }
 
 int fg_world_sync(fg_world *w)

@@ -191,6 +191,11 @@ struct World {
     uint32_t *flush_buf = nullptr;
     size_t flush_bytes = 0;
     int step(uint32_t nsteps, const StepIO *io = nullptr);
+    /* One stage of a step enqueued on its own (FG_RUN_* of the public
+     * header), in the order of the reference's step; staged_done holds the
+     * FG_RUN_* bits (1 << stage) already run in the current step. */
+    uint32_t staged_done = 0;
+    int run_stage(int stage, int flags);
     int step_loop(uint32_t nsteps);
     uint32_t launches_per_step();
     int check();

@@ -317,17 +317,17 @@ __global__ void k_iota_copy(const uint32_t *__restrict__ kin, const uint32_t *__
     }
 }
 
-void radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out, uint32_t n,
-                uint32_t bits, uint32_t digit_bits, const RadixScratch &s, cudaStream_t st)
+cudaError_t radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
+                       uint32_t n, uint32_t bits, uint32_t digit_bits, const RadixScratch &s, cudaStream_t st)
 {
-    if (n == 0) return;
+    if (n == 0) return cudaSuccess;
     if (digit_bits < 1) digit_bits = 1;
     if (digit_bits > 8) digit_bits = 8;
     const int P = radix_passes(bits, digit_bits);
     if (P == 0) {
         if (keys_in != keys_out || vals_in != vals_out || !vals_in)
             k_iota_copy<<<grid_for((n + 255) / 256, 8), 256, 0, st>>>(keys_in, vals_in, keys_out, vals_out, n);
-        return;
+        return cudaSuccess;
     }
     const uint32_t T = (n + RS_TILE - 1) / RS_TILE;
     uint32_t *totals = s.hist + (size_t)RS_RADIX * T;
@@ -349,10 +349,13 @@ void radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys
         vin = vo;
         to_out = !to_out;
     }
+    cudaError_t e = cudaSuccess;
     if (kin != keys_out) {
-        cudaMemcpyAsync(keys_out, kin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
-        cudaMemcpyAsync(vals_out, vin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+        e = cudaMemcpyAsync(keys_out, kin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+        const cudaError_t e2 = cudaMemcpyAsync(vals_out, vin, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = e2;
     }
+    return e;
 }
 
 /* ---------------------------------------------------------- onesweep

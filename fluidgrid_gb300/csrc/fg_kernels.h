@@ -50,8 +50,10 @@ bool onesweep_sort(const uint32_t *keys_in, uint32_t *keys_out, uint32_t *vals_o
                    uint32_t digit_bits, const RadixScratch &s, uint32_t *os, uint32_t *err, cudaStream_t st);
 /* Stable ascending sort of (key, value) by the low `bits` bits of the key.
  * vals_in == nullptr means values 0..n-1.  keys_out/vals_out may alias
- * keys_in/vals_in (in-place). */
-void radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
+ * keys_in/vals_in (in-place).  Returns the status of the device-to-device
+ * copies an odd pass count in place ends with (kernel launch errors are
+ * left for cudaGetLastError). */
+cudaError_t radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
                 uint32_t n, uint32_t bits, uint32_t digit_bits, const RadixScratch &s, cudaStream_t st);
 
 /* start[] must be pre-filled with 0xffffffff over the bucket range.

@@ -135,6 +135,7 @@ void RigidBodySimulator::reset()
     mDynamic.clear();
     mStatic.clear();
     mCoupled = nullptr;
+    mInteractionStarted = false;
 }
 
 void RigidBodySimulator::release() { reset(); }
@@ -147,6 +148,51 @@ int RigidBodySimulator::getNumStaticParticles()
 }
 
 int RigidBodySimulator::getNumStaticRigidBodies() { return (int)mStatic.size(); }
+
+int RigidBodySimulator::startInteraction()
+{
+    if (mInteractionStarted) return FG_E_STATE; /* RigidBodySimulator.cpp:313-323 asserts the same */
+    mInteractionStarted = true;
+    return FG_OK;
+}
+
+int RigidBodySimulator::endInteraction()
+{
+    if (!mInteractionStarted) return FG_E_STATE;
+    mInteractionStarted = false;
+    return FG_OK;
+}
+
+/* One rigid stage on the coupled fluid's world (built, or rebuilt with the
+ * current bodies, by HeterogeneousSimulator::prepare). */
+int RigidBodySimulator::coupled_stage(int stage)
+{
+    if (!mInteractionStarted) return FG_E_STATE;
+    const int r = HeterogeneousSimulator::instance()->prepare();
+    if (r != FG_OK) return r;
+    if (!mCoupled || !mCoupled->world()) return FG_E_STATE;
+    return fg_world_run_stage(mCoupled->world(), stage, 0);
+}
+
+int RigidBodySimulator::generateCollisionData() { return coupled_stage(FG_RUN_RB_GRID); }
+
+int RigidBodySimulator::calculateRigidBodyForcesFromFluid(float4 *pos, float4 *vel, unsigned int *start,
+                                                          unsigned int *end)
+{
+    if (!mInteractionStarted) return FG_E_STATE;
+    int r = HeterogeneousSimulator::instance()->prepare();
+    if (r != FG_OK) return r;
+    Fluid::GPUSPHFluid *f = mCoupled;
+    if (!f || !f->world()) return FG_E_STATE;
+    const bool pos_ok = pos == f->getOrderedPosition() || pos == f->getPosition();
+    const bool vel_ok = vel == f->getOrderedVelocities() || vel == f->getVelocity();
+    if (!pos_ok || !vel_ok || start != f->getHashStart() || end != f->getHashEnd()) return FG_E_INVALID;
+    return fg_world_run_stage(f->world(), FG_RUN_RB_FROM_FLUID, 0);
+}
+
+int RigidBodySimulator::calculateRigidBodyForcesFromRB() { return coupled_stage(FG_RUN_RB_FROM_RB); }
+int RigidBodySimulator::applyForces() { return coupled_stage(FG_RUN_BODY_SUMS); }
+int RigidBodySimulator::integrate() { return coupled_stage(FG_RUN_BODY_INTEGRATE); }
 
 int RigidBodySimulator::getBodyState(double *x4, double *v4, double *q4, double *L4)
 {
@@ -191,7 +237,7 @@ void HeterogeneousSimulator::addSphFluid(Fluid::GPUSPHFluid *fluid)
     if (fluid) mFluids.push_back(fluid);
 }
 
-int HeterogeneousSimulator::doTimeStep()
+int HeterogeneousSimulator::prepare()
 {
     RigidBodySimulator *rbs = RigidBodySimulator::instance();
     const bool bodies = !rbs->mDynamic.empty() || !rbs->mStatic.empty();
@@ -205,7 +251,48 @@ int HeterogeneousSimulator::doTimeStep()
             if (r != FG_OK) return r;
             if (want) rbs->mCoupled = f;
         }
-        const int r = fg_world_step(f->mWorld, 1);
+    }
+    return FG_OK;
+}
+
+int HeterogeneousSimulator::fluid_stage(Fluid::GPUSPHFluid *fluid, int stage, int flags)
+{
+    if (!fluid) return FG_E_INVALID;
+    const int r = prepare();
+    if (r != FG_OK) return r;
+    if (!fluid->mWorld) return FG_E_STATE;
+    return fg_world_run_stage(fluid->mWorld, stage, flags);
+}
+
+int HeterogeneousSimulator::findFluidNeighbourhood(Fluid::GPUSPHFluid *f)
+{
+    return fluid_stage(f, FG_RUN_NEIGHBOURHOOD, 0);
+}
+
+int HeterogeneousSimulator::calculateFluidDensity(Fluid::GPUSPHFluid *f) { return fluid_stage(f, FG_RUN_DENSITY, 0); }
+
+int HeterogeneousSimulator::calculateFluidForces(Fluid::GPUSPHFluid *f, bool useStaticRB, bool useDynamicRB)
+{
+    int flags = 0;
+    if (f && f->mHasBodies) {
+        RigidBodySimulator *rbs = RigidBodySimulator::instance();
+        const bool has_s = !rbs->mStatic.empty(), has_d = !rbs->mDynamic.empty();
+        const bool any = (has_s && useStaticRB) || (has_d && useDynamicRB);
+        const bool all = (!has_s || useStaticRB) && (!has_d || useDynamicRB);
+        if (any && !all) return FG_E_UNSUPPORTED;
+        if (any) flags = FG_RUN_WITH_CONTACT;
+    }
+    return fluid_stage(f, FG_RUN_FORCES, flags);
+}
+
+int HeterogeneousSimulator::integrateFluidForces(Fluid::GPUSPHFluid *f) { return fluid_stage(f, FG_RUN_INTEGRATE, 0); }
+
+int HeterogeneousSimulator::doTimeStep()
+{
+    int r0 = prepare();
+    if (r0 != FG_OK) return r0;
+    for (size_t i = 0; i < mFluids.size(); i++) {
+        const int r = fg_world_step(mFluids[i]->mWorld, 1);
         if (r != FG_OK) return r;
     }
     for (auto *f : mFluids) {

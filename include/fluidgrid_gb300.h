@@ -102,6 +102,29 @@ int fg_world_destroy(fg_world *w);
 /* Enqueue nsteps steps on the world's stream (CUDA-graph replay after the
  * first call).  Returns without waiting. */
 int fg_world_step(fg_world *w, uint32_t nsteps);
+/* One stage of a step, enqueued on the world's stream on its own, for host
+ * code that sequences the step itself as the reference's two-way step does
+ * (HeterogeneousSimulator.cpp:57-126, RigidBodySimulator.cpp:313-611).
+ * Stages run in this order; FG_RUN_INTEGRATE ends the step.  A stage whose
+ * inputs were not made earlier in the same step returns FG_E_STATE (the
+ * rigid stages do nothing in a world without bodies), and fg_world_step
+ * returns FG_E_STATE while a staged step is unfinished.  The kernels are
+ * those of fg_world_step, so a staged step gives the same bits; no graph is
+ * captured and no autotuning round runs.  flags: FG_RUN_WITH_CONTACT for
+ * FG_RUN_FORCES adds the rigid contact term (a whole step always does). */
+enum {
+    FG_RUN_NEIGHBOURHOOD = 1, /* hash, sort, cell ranges + sorted gather */
+    FG_RUN_DENSITY = 2,
+    FG_RUN_RB_GRID = 3,        /* sphere world positions, keys, sort, ranges */
+    FG_RUN_RB_FROM_FLUID = 4,  /* sphere force/torque from the fluid */
+    FG_RUN_RB_FROM_RB = 5,     /* + sphere/sphere contact between bodies */
+    FG_RUN_FORCES = 6,         /* pressure, viscosity, walls (+ contact): velocities */
+    FG_RUN_BODY_SUMS = 7,      /* FP64 per-body force/torque sums */
+    FG_RUN_BODY_INTEGRATE = 8, /* FP64 body integration */
+    FG_RUN_INTEGRATE = 9       /* particle positions; ends the step */
+};
+enum { FG_RUN_WITH_CONTACT = 1 };
+int fg_world_run_stage(fg_world *w, int stage, int flags);
 /* Wait for the world's stream; returns FG_E_NONFINITE if the last
  * fg_world_check found NaN/Inf, FG_E_CUDA on a CUDA error. */
 int fg_world_sync(fg_world *w);
@@ -269,13 +292,15 @@ int fg_probe_fp32_peak(float *tflops);
 
 /* Stable in-place sort of n (key, value) pairs by the low keyBits bits of the
  * key -- the same result as fgc_sort_pairs -- without allocating: its scratch
- * is a fixed ~8.65 MB array inside the library (held on every GPU that loads
- * it), for callers that cannot call cudaMalloc/cudaFree while they sort (a
+ * is a fixed 8,913,920-byte (8.91 MB) array inside the library (held on every
+ * GPU that loads it), for callers that cannot call cudaMalloc/cudaFree while they sort (a
  * host that gives all device memory to its own pool, a step loop that must
  * not wait for the allocator).  No counterpart in the reference.
  * n <= 1,048,576 (larger n -> FG_E_INVALID).  All calls share the scratch:
- * calls that overlap on the GPU race, so serialise them.  The first call on a
- * device looks up the scratch address; make it before any stream capture.
+ * calls that overlap on the GPU race, so serialise them.  Each call outside
+ * stream capture looks up the scratch address on the current device; a call
+ * during capture reuses the last one, so make the first call on a device
+ * before any stream capture (else FG_E_STATE).
  * Work is enqueued on `stream` (NULL = legacy default stream). */
 int fg_sort_pairs_noalloc(unsigned int *keys, unsigned int *values, unsigned int keyBits, unsigned int n,
                           fg_stream_t stream);

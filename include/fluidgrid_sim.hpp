@@ -17,8 +17,27 @@
 // two-way coupling with the RigidBodySimulator's bodies, the reference's
 // commented block HeterogeneousSimulator.cpp:57-126) as one captured graph.
 // Device pointers returned by the getters are owned by the fluid and stay
-// valid until it is destroyed, except that the first doTimeStep() after
-// bodies were added rebuilds the fluid's world (and its buffers).
+// valid until it is destroyed, except that the first doTimeStep() (or stage
+// call) after bodies were added rebuilds the fluid's world (and its buffers).
+//
+// Host code that sequences the step itself, as the reference's commented
+// two-way block does, calls the stage methods instead of doTimeStep():
+//   RigidBodySimulator::startInteraction();
+//   HeterogeneousSimulator::findFluidNeighbourhood(f);
+//   HeterogeneousSimulator::calculateFluidDensity(f);
+//   RigidBodySimulator::generateCollisionData();
+//   RigidBodySimulator::calculateRigidBodyForcesFromFluid(...);
+//   RigidBodySimulator::calculateRigidBodyForcesFromRB();   (bodies that touch)
+//   HeterogeneousSimulator::calculateFluidForces(f, useStaticRB, useDynamicRB);
+//   RigidBodySimulator::applyForces();
+//   RigidBodySimulator::integrate();
+//   HeterogeneousSimulator::integrateFluidForces(f);
+//   RigidBodySimulator::endInteraction();
+// Each enqueues one stage of the coupled world (fg_world_run_stage) and
+// returns 0 or an fg_status: FG_E_STATE when a stage's inputs were not made
+// earlier in the same step.  The stages run the kernels of doTimeStep(), so
+// the result is the same bits.  The reference's methods return void; these
+// return the status, which callers may ignore.
 #ifndef FLUIDGRID_SIM_HPP
 #define FLUIDGRID_SIM_HPP
 
@@ -238,20 +257,38 @@ public:
     int getNumStaticRigidBodies();
     int getNumDynamicRigidBodies() { return (int)mDynamic.size(); }
 
-    // The collision-data build, the rigid-body forces from the fluid and
-    // from other bodies, the per-body reduction and the integration run
-    // inside each coupled fluid's step (HeterogeneousSimulator::doTimeStep);
-    // called on their own they do nothing.
-    void generateCollisionData() {}
-    void startInteraction() {}
-    void endInteraction() {}
-    void calculateRigidBodyForcesFromRB() {}
-    void calculateRigidBodyForcesFromFluid(float4 *, float4 *, unsigned int *, unsigned int *) {}
-    void applyForces() {}
-    void integrate() {}
+    // Stages of the two-way step on the coupled fluid's world (the first
+    // fluid added to the HeterogeneousSimulator), in the order of
+    // RigidBodySimulator.cpp:313-611.  doTimeStep() runs them all itself.
+    //   startInteraction/endInteraction  bracket one step (FG_E_STATE when
+    //                                    started twice or ended unstarted)
+    //   generateCollisionData            sphere world positions, keys, sort,
+    //                                    cell ranges of every body (resident:
+    //                                    no host broad phase or upload)
+    //   calculateRigidBodyForcesFromFluid  sphere force/torque from the fluid;
+    //                                    the arguments must be the coupled
+    //                                    fluid's buffers (its sorted or, as
+    //                                    the reference's commented call passes
+    //                                    them, unsorted positions/velocities
+    //                                    and its start/end): the fluid's grid
+    //                                    is used either way
+    //   calculateRigidBodyForcesFromRB   + contact with the other bodies and
+    //                                    with static ones (mass 0)
+    //   applyForces                      FP64 per-body force/torque sums
+    //   integrate                        FP64 body integration
+    int generateCollisionData();
+    int startInteraction();
+    int endInteraction();
+    int calculateRigidBodyForcesFromRB();
+    int calculateRigidBodyForcesFromFluid(float4 *dfluidParticlePos, float4 *dfluidParticleVel,
+                                          unsigned int *dfluidHashStart, unsigned int *dfluidHashEnd);
+    int applyForces();
+    int integrate();
 
     // FP64 body state after the last step of the fluid the bodies are
-    // coupled to: x (position), v, q (orientation), L per body, 4 doubles each
+    // coupled to: x (position), v, q (orientation), L per body, 4 doubles
+    // each, so every non-null array holds 4 x (dynamic + static bodies)
+    // doubles; dynamic bodies come first, in the order they were added
     int getBodyState(double *x4, double *v4, double *q4, double *L4);
 
     const std::vector<RigidBody *> &dynamicBodies() { return mDynamic; }
@@ -261,8 +298,10 @@ private:
     RigidBodySimulator() {}
     friend class HeterogeneousSimulator;
     friend class Fluid::GPUSPHFluid;
+    int coupled_stage(int stage);
     std::vector<RigidBody *> mDynamic, mStatic;
     Fluid::GPUSPHFluid *mCoupled = nullptr;
+    bool mInteractionStarted = false;
 };
 
 class HeterogeneousSimulator {
@@ -275,8 +314,22 @@ public:
     // RigidBodySimulator holds bodies.  Returns 0 or an fg_status.
     int doTimeStep();
 
+    // The fluid stages of doTimeStep (private in the reference, public here
+    // for host code that sequences the two-way step itself).  With bodies,
+    // calculateFluidForces adds the contact term when the flags ask for every
+    // kind of body present (static = mass 0, dynamic); asking for only one of
+    // two kinds present returns FG_E_UNSUPPORTED, since both share one grid.
+    // integrateFluidForces ends the step.
+    int findFluidNeighbourhood(Fluid::GPUSPHFluid *fluid);
+    int calculateFluidDensity(Fluid::GPUSPHFluid *fluid);
+    int calculateFluidForces(Fluid::GPUSPHFluid *fluid, bool useStaticRB, bool useDynamicRB);
+    int integrateFluidForces(Fluid::GPUSPHFluid *fluid);
+
 private:
     HeterogeneousSimulator();
+    friend class RigidBodySimulator;
+    int prepare(); /* (re)build the fluids' worlds for the current bodies */
+    int fluid_stage(Fluid::GPUSPHFluid *fluid, int stage, int flags);
     std::vector<Fluid::GPUSPHFluid *> mFluids;
 };
 

@@ -24,4 +24,7 @@ def build_and_run(src, args=(), cwd=None):
         f.write(src)
     subprocess.check_call(["g++", "-std=c++17", "-O1", "-I", INC, "-I", CUDA_INC, cpp, "-o", exe, "-L", LIBDIR,
                            "-lfluidgrid_gb300", "-Wl,-rpath," + LIBDIR])
-    return subprocess.run([exe] + list(args), cwd=d, capture_output=True, text=True, check=True).stdout
+    r = subprocess.run([exe] + list(args), cwd=d, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("program exited with %d; stderr:\n%s" % (r.returncode, r.stderr[-4000:]))
+    return r.stdout

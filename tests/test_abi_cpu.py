@@ -176,3 +176,12 @@ def test_option_and_status_codes_match_header():
     status = _header_enum("FG_E_")
     status["FG_OK"] = _header_enum("FG_OK")["FG_OK"]
     assert {v: k for k, v in _ffi.STATUS.items()} == status
+
+
+def test_run_stage_codes_match_header():
+    run = _header_enum("FG_RUN_")
+    contact = run.pop("FG_RUN_WITH_CONTACT")
+    assert {"FG_RUN_" + k.upper(): v for k, v in _ffi.RUN.items()} == run
+    assert contact == _ffi.RUN_WITH_CONTACT
+    # the stages are numbered in step order, from 1
+    assert sorted(run.values()) == list(range(1, len(run) + 1))
