@@ -108,7 +108,8 @@ RUN_WITH_CONTACT = 1
 
 OPTIONS = {"neighbor_list": 1, "target_order": 2, "order_period": 3, "digit_bits": 4, "kernel": 5,
            "autotune_period": 6, "autotune_kernels": 7, "list_cap": 8, "ctas_per_sm": 10,
-           "autotune_tiles": 11, "list_autogrow": 12, "graph_steps": 13, "one_pass_sort": 14}
+           "autotune_tiles": 11, "list_autogrow": 12, "graph_steps": 13, "one_pass_sort": 14, "block_size": 16,
+           "runs_per_cta": 17}
 NUM_KERNELS = 3
 
 STATUS = {0: "FG_OK", 1: "FG_E_INVALID", 2: "FG_E_CUDA", 3: "FG_E_OOM", 4: "FG_E_BUDGET", 5: "FG_E_NONFINITE",

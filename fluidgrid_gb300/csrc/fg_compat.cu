@@ -67,7 +67,7 @@ FgScene fluid_scene()
 
 fg::Launch single_launch(const FgScene *S, uint32_t n)
 {
-    fg::Launch L;
+    fg::Launch L{}; /* default launch shape: 64 CTAs of 128 threads per SM */
     L.table = nullptr;
     L.single = S;
     L.work = nullptr;

@@ -561,7 +561,7 @@ int World::create(const fg_scene_desc *d, uint32_t ns, cudaStream_t st)
 
 Launch World::fluid_launch() const
 {
-    Launch L;
+    Launch L{};
     L.table = single ? nullptr : scenes_d;
     L.single = &scenes_h[0];
     L.work = single ? nullptr : work_d;
@@ -569,12 +569,13 @@ Launch World::fluid_launch() const
     L.n = n;
     L.stream = stream;
     L.ctas_per_sm = ctas_per_sm;
+    L.block = block;
     return L;
 }
 
 Launch World::sphere_launch() const
 {
-    Launch L;
+    Launch L{};
     L.table = single ? nullptr : scenes_d;
     L.single = &scenes_h[0];
     L.work = single ? nullptr : work_sph_d;
@@ -737,7 +738,7 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         mark(3, 0);
         if (use_cc)
             launch_density_cc(single ? nullptr : scenes_d, &scenes_h[0], nscenes, runs, nruns, keys, spos, svel, start,
-                              end, dp, nbr.rec, n, stream);
+                              end, dp, nbr.rec, n, stream, cc_warps);
         else
             launch_density(L, spos, start, end, dp, 0.f, 0.f, 0.f, 0, svel, use_list ? &nbr : nullptr,
                            target_order(), pair_counter);
@@ -765,7 +766,7 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         o.pos = fused_integrate ? pos : nullptr;
         if (use_cc)
             launch_forces_cc(single ? nullptr : scenes_d, &scenes_h[0], nscenes, runs, nruns, keys, spos, svel,
-                             nbr.rec, start, end, ids, o, rb ? &G : nullptr, n, stream);
+                             nbr.rec, start, end, ids, o, rb ? &G : nullptr, n, stream, cc_warps);
         else
             launch_forces(L, spos, svel, dp, start, end, ids, o, rb ? &G : nullptr, nullptr, 0.f, 0.f, 0,
                           use_list ? &nbr : nullptr, target_order());
@@ -811,7 +812,7 @@ uint64_t World::graph_signature() const
     return (uint64_t)((stages & 0xffu) | (fused_integrate ? 0x100u : 0u) | (digit_bits << 9) |
                       (use_list ? 0x10000u : 0u) | ((use_order && order_valid) ? 0x20000u : 0u) |
                       (use_cc ? 0x40000u : 0u) | ((ctas_per_sm & 0x7fu) << 20) |
-                      (one_pass_sort ? 0x8000000u : 0u)) |
+                      (one_pass_sort ? 0x8000000u : 0u) | ((block >> 6) << 28) | ((cc_warps & 0x7u) << 24)) |
            ((uint64_t)nbr.stride << 32);
 }
 
@@ -903,11 +904,13 @@ int World::graph_for_current(cudaGraphExec_t *out, uint32_t nsteps)
  * step() calls. */
 void World::tune_begin()
 {
-    int dims[4], nd = 0;
+    int dims[6], nd = 0;
     if (__builtin_popcount(tune_kernels & 0x7u) >= 2) dims[nd++] = 0;
     if ((tune_tiles & 1u) && !use_cc) dims[nd++] = 1;
     if (tune_tiles & 2u) dims[nd++] = 2;
     if (tune_tiles & 4u) dims[nd++] = 3;
+    if ((tune_tiles & 8u) && !use_cc) dims[nd++] = 4;
+    if ((tune_tiles & 16u) && use_cc) dims[nd++] = 5;
     tr.ncand = 0;
     if (!nd) return;
     tr.dim = dims[tune_round++ % (uint32_t)nd];
@@ -920,11 +923,19 @@ void World::tune_begin()
         for (int k = 0; k < 3; k++) tr.cand[tr.ncand++] = v[k];
     } else if (tr.dim == 2) {
         for (int v = 6; v <= 8; v++) tr.cand[tr.ncand++] = v;
-    } else {
+    } else if (tr.dim == 3) {
         /* the sort: three kernels per pass (faster for ~1M keys and more)
          * or one (faster for small scenes) */
         tr.cand[tr.ncand++] = 0;
         tr.cand[tr.ncand++] = 1;
+    } else if (tr.dim == 4) {
+        /* threads per CTA of the density/force grids */
+        const int v[3] = {64, 128, 256};
+        for (int k = 0; k < 3; k++) tr.cand[tr.ncand++] = v[k];
+    } else {
+        /* bucket runs (warps) per CTA of kernel 2 */
+        const int v[3] = {1, 2, 4};
+        for (int k = 0; k < 3; k++) tr.cand[tr.ncand++] = v[k];
     }
     if (tr.ncand < 2) {
         tr.ncand = 0;
@@ -937,8 +948,9 @@ void World::tune_begin()
                 tr.ncand = 0;
                 return;
             }
-    tr.prev = tr.dim == 0 ? current_kernel()
-                          : (tr.dim == 1 ? (int)ctas_per_sm : (tr.dim == 2 ? (int)digit_bits : (one_pass_sort ? 1 : 0)));
+    const int prev[6] = {current_kernel(), (int)ctas_per_sm, (int)digit_bits, one_pass_sort ? 1 : 0, (int)block,
+                         (int)cc_warps};
+    tr.prev = prev[tr.dim];
     tr.idx = 0;
     tr.active = true;
 }
@@ -948,7 +960,9 @@ void World::tune_apply(int dim, int v)
     if (dim == 0) set_kernel(v);
     else if (dim == 1) ctas_per_sm = (uint32_t)v;
     else if (dim == 2) digit_bits = (uint32_t)v;
-    else one_pass_sort = v != 0;
+    else if (dim == 3) one_pass_sort = v != 0;
+    else if (dim == 4) block = (uint32_t)v;
+    else cc_warps = (uint32_t)v;
 }
 
 int World::tune_finish()
@@ -1122,7 +1136,7 @@ int World::run_stage(int stage, int flags)
         if (!need(bit(FG_RUN_NEIGHBOURHOOD), "FG_RUN_DENSITY needs FG_RUN_NEIGHBOURHOOD first")) return FG_E_STATE;
         if (use_cc)
             launch_density_cc(single ? nullptr : scenes_d, &scenes_h[0], nscenes, runs, nruns, keys, spos, svel, start,
-                              end, dp, nbr.rec, n, stream);
+                              end, dp, nbr.rec, n, stream, cc_warps);
         else
             launch_density(L, spos, start, end, dp, 0.f, 0.f, 0.f, 0, svel, use_list ? &nbr : nullptr,
                            target_order(), pair_counter);
@@ -1178,7 +1192,7 @@ int World::run_stage(int stage, int flags)
         o.pos = nullptr; /* FG_RUN_INTEGRATE moves the particles */
         if (use_cc)
             launch_forces_cc(single ? nullptr : scenes_d, &scenes_h[0], nscenes, runs, nruns, keys, spos, svel,
-                             nbr.rec, start, end, ids, o, contact ? &G : nullptr, n, stream);
+                             nbr.rec, start, end, ids, o, contact ? &G : nullptr, n, stream, cc_warps);
         else
             launch_forces(L, spos, svel, dp, start, end, ids, o, contact ? &G : nullptr, nullptr, 0.f, 0.f, 0,
                           use_list ? &nbr : nullptr, target_order());
@@ -1768,12 +1782,20 @@ int fg_world_set_option(fg_world *w, int option, int value)
         W->graph_steps = (uint32_t)value;
         return FG_OK;
     case FG_OPT_ONE_PASS_SORT: W->one_pass_sort = value != 0; return FG_OK;
+    case FG_OPT_BLOCK_SIZE:
+        if (value != 64 && value != 128 && value != 256) return FG_E_INVALID;
+        W->block = (uint32_t)value;
+        return FG_OK;
+    case FG_OPT_RUNS_PER_CTA:
+        if (value != 1 && value != 2 && value != 4) return FG_E_INVALID;
+        W->cc_warps = (uint32_t)value;
+        return FG_OK;
     case FG_OPT_CTAS_PER_SM:
         if (value < 0 || value > 64) return FG_E_INVALID;
         W->ctas_per_sm = (uint32_t)value;
         return FG_OK;
     case FG_OPT_AUTOTUNE_TILES:
-        if (value < 0 || value > 7) return FG_E_INVALID;
+        if (value < 0 || value > 31) return FG_E_INVALID;
         W->tune_tiles = (uint32_t)value;
         return FG_OK;
     default: return FG_E_INVALID;
@@ -1830,6 +1852,8 @@ int fg_world_get_option(const fg_world *w, int option, int *value)
     case FG_OPT_ORDER_PERIOD: *value = (int)W->order_period; return FG_OK;
     case FG_OPT_DIGIT_BITS: *value = (int)W->digit_bits; return FG_OK;
     case FG_OPT_KERNEL: *value = W->current_kernel(); return FG_OK;
+    case FG_OPT_BLOCK_SIZE: *value = (int)W->block; return FG_OK;
+    case FG_OPT_RUNS_PER_CTA: *value = (int)W->cc_warps; return FG_OK;
     case FG_OPT_AUTOTUNE_PERIOD: *value = (int)W->tune_period; return FG_OK;
     case FG_OPT_AUTOTUNE_KERNELS: *value = (int)W->tune_kernels; return FG_OK;
     case FG_OPT_LIST_CAP: *value = (int)W->list_cap; return FG_OK;

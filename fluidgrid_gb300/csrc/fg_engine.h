@@ -59,6 +59,8 @@ struct World {
     bool use_list = true, use_order = false;
     bool use_cc = false;       /* kernel 2: warp per bucket run, candidates staged in shared memory */
     uint32_t ctas_per_sm = 0;  /* CTAs per SM of the density/force grids (0 = 64) */
+    uint32_t block = 128;      /* kernels 0/1: threads per CTA of the density/force grids (64, 128, 256) */
+    uint32_t cc_warps = 4;     /* kernel 2: bucket runs (warps) per CTA (1, 2, 4) */
     int set_list_cap(uint32_t cap);
     uint32_t *runs = nullptr;  /* occupied-bucket run heads */
     uint32_t *nruns = nullptr; /* device counter */
@@ -139,7 +141,8 @@ struct World {
     uint32_t tune_count[3] = {0, 0, 0}; /* steps run with kernel 0..2 */
     float tune_last_ms[3] = {0.f, 0.f, 0.f};
     uint32_t tune_kernels = 0x2; /* candidate kernels bit mask */
-    uint32_t tune_tiles = 0x7;   /* 1: CTAs per SM, 2: digit width, 4: sort variant */
+    uint32_t tune_tiles = 0x1f;  /* 1: CTAs per SM, 2: digit width, 4: sort variant, 8: block size,
+                                    16: runs per CTA (kernel 2) */
     uint32_t tune_round = 0;
     unsigned long long *overflow_counter = nullptr; /* list overflows since the last reset */
     uint32_t *max_count = nullptr; /* largest list count since the last capacity check */

@@ -18,7 +18,8 @@ struct Launch {
     uint32_t nwork;        /* work items */
     uint32_t n;            /* particles (single-scene mode) */
     cudaStream_t stream;
-    uint32_t ctas_per_sm;  /* density/force grids: CTAs per SM (0 = 64) */
+    uint32_t ctas_per_sm;  /* density/force grids: CTAs of FG_CHUNK threads per SM (0 = 64) */
+    uint32_t block;        /* density/force grids: threads per CTA, 64, 128 or 256 (0 = FG_CHUNK) */
 };
 
 int sm_count();
@@ -141,11 +142,11 @@ void launch_integrate(const Launch &L, float4 *pos, const float4 *vel);
 void launch_density_cc(const FgScene *table, const FgScene *single, uint32_t nscenes, const uint32_t *runs,
                        const uint32_t *nruns, const uint32_t *keys, const float4 *spos, const float4 *svel,
                        const uint32_t *start, const uint32_t *end, float2 *dp, float4 *rec, uint32_t n,
-                       cudaStream_t s);
+                       cudaStream_t s, uint32_t warps = 4);
 void launch_forces_cc(const FgScene *table, const FgScene *single, uint32_t nscenes, const uint32_t *runs,
                       const uint32_t *nruns, const uint32_t *keys, const float4 *spos, const float4 *svel,
                       const float4 *rec, const uint32_t *start, const uint32_t *end, const uint32_t *ids,
-                      ForceOut out, const RigidGrid *rigid, uint32_t n, cudaStream_t s);
+                      ForceOut out, const RigidGrid *rigid, uint32_t n, cudaStream_t s, uint32_t warps = 4);
 
 /* ---- rigid bodies (fg_rigid.cu) ---- */
 void launch_rb_from_fluid(const Launch &Lrb, const float4 *rb_spos, const uint32_t *rb_ids, const float4 *body_vel,

@@ -180,6 +180,8 @@ int Server::relayout()
             nw->list_cap_alloc = w->list_cap_alloc;
             nw->digit_bits = w->digit_bits;
             nw->ctas_per_sm = w->ctas_per_sm;
+            nw->block = w->block;
+            nw->cc_warps = w->cc_warps;
             nw->tune_period = w->tune_period;
             nw->use_graphs = w->use_graphs;
             size_t free_b = 0, total_b = 0;

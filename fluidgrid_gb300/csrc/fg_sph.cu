@@ -41,8 +41,15 @@ namespace fg {
  * the full 64 warps per SM hide the candidate loads and the in-range
  * branch's divergence better than 8 CTAs at 64 registers (0.85 -> 0.71 ms
  * on the 1M-particle dam break). */
-template <bool LIST>
-__global__ void __launch_bounds__(FG_CHUNK, 16) k_density(const FgWork *__restrict__ work, uint32_t nwork,
+/* Work items are FG_CHUNK particles whatever the block size: a CTA of
+ * BLOCK < FG_CHUNK threads takes an item in FG_CHUNK / BLOCK passes, one of
+ * BLOCK > FG_CHUNK threads takes BLOCK / FG_CHUNK items at once.  Every
+ * particle's arithmetic is the same for every block size. */
+#define FG_ITEMS_PER_CTA(B) ((B) >= FG_CHUNK ? (B) / FG_CHUNK : 1u)
+#define FG_PASSES(B) ((B) >= FG_CHUNK ? 1u : FG_CHUNK / (B))
+
+template <bool LIST, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 2048 / BLOCK) k_density(const FgWork *__restrict__ work, uint32_t nwork,
                                                      uint32_t n_single, const FgScene *__restrict__ table,
                                                      const __grid_constant__ FgScene single,
                                                      const float4 *__restrict__ spos,
@@ -53,12 +60,17 @@ __global__ void __launch_bounds__(FG_CHUNK, 16) k_density(const FgWork *__restri
                                                      const __grid_constant__ NbrList list, TargetOrder ord,
                                                      unsigned long long *__restrict__ pairs)
 {
-    const uint32_t tid = threadIdx.x;
+    constexpr uint32_t IPC = FG_ITEMS_PER_CTA(BLOCK), PASSES = FG_PASSES(BLOCK);
+    const uint32_t sub = IPC > 1u ? threadIdx.x / FG_CHUNK : 0u;
+    const uint32_t lt = IPC > 1u ? threadIdx.x % FG_CHUNK : threadIdx.x;
     const uint32_t cap = LIST ? __ldg(list.cap) : 0u;
     unsigned long long pc = 0; /* in-range density visits of this thread */
     uint32_t mx = 0;           /* largest list count of this thread */
     uint32_t ovf = 0;          /* targets of this thread with more entries than slots */
-    for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+    for (uint32_t w = blockIdx.x * IPC + sub; w < nwork; w += gridDim.x * IPC)
+#pragma unroll 1
+    for (uint32_t ps = 0; ps < PASSES; ps++) {
+        const uint32_t tid = lt + ps * BLOCK;
         FgWork it = fg_work(work, w, n_single);
         const bool valid = tid < it.count;
         const FgScene *S = fg_scene(table, &single, it.scene);
@@ -102,18 +114,19 @@ __global__ void __launch_bounds__(FG_CHUNK, 16) k_density(const FgWork *__restri
     }
     /* once per warp: in-range pair visits (self included) for reporting, and
      * the largest list count for the capacity check */
+    const uint32_t lane = threadIdx.x & 31u;
     if (pairs) {
 #pragma unroll
         for (int o = 16; o; o >>= 1) pc += __shfl_xor_sync(0xffffffffu, pc, o);
-        if ((tid & 31) == 0 && pc) atomicAdd(pairs, pc);
+        if (lane == 0 && pc) atomicAdd(pairs, pc);
     }
     if (LIST && list.max_count) {
         mx = __reduce_max_sync(0xffffffffu, mx);
-        if ((tid & 31) == 0 && mx) atomicMax(list.max_count, mx);
+        if (lane == 0 && mx) atomicMax(list.max_count, mx);
     }
     if (LIST && list.overflow) {
         ovf = __reduce_add_sync(0xffffffffu, ovf);
-        if ((tid & 31) == 0 && ovf) atomicAdd(list.overflow, (unsigned long long)ovf);
+        if (lane == 0 && ovf) atomicAdd(list.overflow, (unsigned long long)ovf);
     }
 }
 
@@ -122,16 +135,26 @@ void launch_density(const Launch &L, const float4 *spos, const uint32_t *start, 
                     TargetOrder ord, unsigned long long *pairs)
 {
     if (!L.nwork) return;
-    const uint32_t g = grid_for(L.nwork, L.ctas_per_sm ? (int)L.ctas_per_sm : 64);
-    if (list) {
-        k_density<true><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, start,
-                                                      end, dp, gas_o, rest_o, mass_o, use_o, *list, ord, pairs);
+    NbrList none;
+    memset(&none, 0, sizeof(none));
+    const NbrList &nl = list ? *list : none;
+    const uint32_t B = L.block ? L.block : FG_CHUNK;
+    const uint32_t ipc = FG_ITEMS_PER_CTA(B);
+    /* ctas_per_sm counts CTAs of FG_CHUNK threads: the same threads per SM
+     * for every block size */
+    const int per_sm = (int)(((L.ctas_per_sm ? L.ctas_per_sm : 64u) * FG_CHUNK) / B);
+    const uint32_t g = grid_for((L.nwork + ipc - 1u) / ipc, per_sm > 0 ? per_sm : 1);
+#define FG_DENSITY(LI, BL)                                                                                        \
+    k_density<LI, BL><<<g, BL, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, start, end, dp, \
+                                              gas_o, rest_o, mass_o, use_o, nl, ord, pairs)
+    if (B == 64u) {
+        if (list) FG_DENSITY(true, 64); else FG_DENSITY(false, 64);
+    } else if (B == 256u) {
+        if (list) FG_DENSITY(true, 256); else FG_DENSITY(false, 256);
     } else {
-        NbrList none;
-        memset(&none, 0, sizeof(none));
-        k_density<false><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, start,
-                                                       end, dp, gas_o, rest_o, mass_o, use_o, none, ord, pairs);
+        if (list) FG_DENSITY(true, 128); else FG_DENSITY(false, 128);
     }
+#undef FG_DENSITY
 }
 
 struct RigidArgs {
@@ -140,8 +163,8 @@ struct RigidArgs {
     int use_dyn, use_sta;
 };
 
-template <bool LIST>
-__global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ work, uint32_t nwork,
+template <bool LIST, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 768 / BLOCK) k_forces(const FgWork *__restrict__ work, uint32_t nwork,
                                                     uint32_t n_single, const FgScene *__restrict__ table,
                                                     const __grid_constant__ FgScene single,
                                                     const float4 *__restrict__ spos, const float4 *__restrict__ svel,
@@ -153,11 +176,17 @@ __global__ void __launch_bounds__(FG_CHUNK) k_forces(const FgWork *__restrict__ 
                                                     const __grid_constant__ RigidArgs R, float mass_o, float visc_o,
                                                     int use_o, const __grid_constant__ NbrList list, TargetOrder ord)
 {
-    for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+    constexpr uint32_t IPC = FG_ITEMS_PER_CTA(BLOCK), PASSES = FG_PASSES(BLOCK);
+    const uint32_t sub = IPC > 1u ? threadIdx.x / FG_CHUNK : 0u;
+    const uint32_t lt = IPC > 1u ? threadIdx.x % FG_CHUNK : threadIdx.x;
+    for (uint32_t w = blockIdx.x * IPC + sub; w < nwork; w += gridDim.x * IPC)
+#pragma unroll 1
+    for (uint32_t ps = 0; ps < PASSES; ps++) {
+        const uint32_t tid = lt + ps * BLOCK;
         FgWork it = fg_work(work, w, n_single);
-        if (threadIdx.x >= it.count) continue;
+        if (tid >= it.count) continue;
         const FgScene *S = fg_scene(table, &single, it.scene);
-        const uint32_t tpos = it.first + threadIdx.x; /* target slot */
+        const uint32_t tpos = it.first + tid; /* target slot */
         const uint32_t pid = ord.tord ? __ldg(ord.tord + tpos) : 0u;
         const uint32_t i = ord.tord ? __ldg(ord.inv + pid) : tpos;
         const float4 p = spos[i];
@@ -286,17 +315,24 @@ void launch_forces(const Launch &L, const float4 *spos, const float4 *svel, cons
     memset(&R, 0, sizeof(R));
     if (rigid) { R.dyn = *rigid; R.use_dyn = 1; }
     if (statics) { R.sta = *statics; R.use_sta = 1; }
-    const uint32_t g = grid_for(L.nwork, L.ctas_per_sm ? (int)L.ctas_per_sm : 64);
-    if (list) {
-        k_forces<true><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, dp, start,
-                                                     end, ids, out.vel, out.pos, R, mass_o, visc_o, use_o, *list, ord);
+    NbrList none;
+    memset(&none, 0, sizeof(none));
+    const NbrList &nl = list ? *list : none;
+    const uint32_t B = L.block ? L.block : FG_CHUNK;
+    const uint32_t ipc = FG_ITEMS_PER_CTA(B);
+    const int per_sm = (int)(((L.ctas_per_sm ? L.ctas_per_sm : 64u) * FG_CHUNK) / B);
+    const uint32_t g = grid_for((L.nwork + ipc - 1u) / ipc, per_sm > 0 ? per_sm : 1);
+#define FG_FORCES(LI, BL)                                                                                        \
+    k_forces<LI, BL><<<g, BL, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, dp, start, end, \
+                                             ids, out.vel, out.pos, R, mass_o, visc_o, use_o, nl, ord)
+    if (B == 64u) {
+        if (list) FG_FORCES(true, 64); else FG_FORCES(false, 64);
+    } else if (B == 256u) {
+        if (list) FG_FORCES(true, 256); else FG_FORCES(false, 256);
     } else {
-        NbrList none;
-        memset(&none, 0, sizeof(none));
-        k_forces<false><<<g, FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, spos, svel, dp,
-                                                      start, end, ids, out.vel, out.pos, R, mass_o, visc_o, use_o,
-                                                      none, ord);
+        if (list) FG_FORCES(true, 128); else FG_FORCES(false, 128);
     }
+#undef FG_FORCES
 }
 
 /* SPHIntegrateK (K_FluidSim.cu:418-438): pos += vel*(dt/scale) for active

@@ -32,7 +32,7 @@
 
 namespace fg {
 
-#define CC_WARPS 4
+/* warps (bucket runs in flight) per CTA: 1, 2 or 4, an autotuner dimension */
 #define CC_CAP 256
 
 struct CcArgs {
@@ -83,6 +83,7 @@ __device__ __forceinline__ void cc_stage(uint32_t st, uint32_t off, uint32_t c0,
     __syncwarp();
 }
 
+template <int CC_WARPS>
 __global__ void __launch_bounds__(CC_WARPS * 32) k_density_cc(const FgScene *__restrict__ table,
                                                              const __grid_constant__ FgScene single,
                                                              const __grid_constant__ CcArgs A,
@@ -182,6 +183,7 @@ struct CcForceArgs {
     const uint32_t *ids;
 };
 
+template <int CC_WARPS>
 __global__ void __launch_bounds__(CC_WARPS * 32) k_forces_cc(const FgScene *__restrict__ table,
                                                             const __grid_constant__ FgScene single,
                                                             const __grid_constant__ CcArgs A,
@@ -302,7 +304,7 @@ __global__ void __launch_bounds__(CC_WARPS * 32) k_forces_cc(const FgScene *__re
 void launch_density_cc(const FgScene *table, const FgScene *single, uint32_t nscenes, const uint32_t *runs,
                        const uint32_t *nruns, const uint32_t *keys, const float4 *spos, const float4 *svel,
                        const uint32_t *start, const uint32_t *end, float2 *dp, float4 *rec, uint32_t n,
-                       cudaStream_t s)
+                       cudaStream_t s, uint32_t warps)
 {
     if (!n) return;
     CcArgs A;
@@ -310,14 +312,16 @@ void launch_density_cc(const FgScene *table, const FgScene *single, uint32_t nsc
     A.nruns = nruns;
     A.keys = keys;
     A.nscenes = nscenes;
-    const uint32_t g = (uint32_t)sm_count() * 8u;
-    k_density_cc<<<g, CC_WARPS * 32, 0, s>>>(table, *single, A, spos, svel, start, end, dp, rec);
+    /* 32 warps per SM whatever the CTA size */
+    if (warps == 1u) k_density_cc<1><<<sm_count() * 32u, 32, 0, s>>>(table, *single, A, spos, svel, start, end, dp, rec);
+    else if (warps == 2u) k_density_cc<2><<<sm_count() * 16u, 64, 0, s>>>(table, *single, A, spos, svel, start, end, dp, rec);
+    else k_density_cc<4><<<sm_count() * 8u, 128, 0, s>>>(table, *single, A, spos, svel, start, end, dp, rec);
 }
 
 void launch_forces_cc(const FgScene *table, const FgScene *single, uint32_t nscenes, const uint32_t *runs,
                       const uint32_t *nruns, const uint32_t *keys, const float4 *spos, const float4 *svel,
                       const float4 *rec, const uint32_t *start, const uint32_t *end, const uint32_t *ids,
-                      ForceOut out, const RigidGrid *rigid, uint32_t n, cudaStream_t s)
+                      ForceOut out, const RigidGrid *rigid, uint32_t n, cudaStream_t s, uint32_t warps)
 {
     if (!n) return;
     CcArgs A;
@@ -334,8 +338,10 @@ void launch_forces_cc(const FgScene *table, const FgScene *single, uint32_t nsce
     O.vel_out = out.vel;
     O.pos_out = out.pos;
     O.ids = ids;
-    const uint32_t g = (uint32_t)sm_count() * 4u;
-    k_forces_cc<<<g, CC_WARPS * 32, 0, s>>>(table, *single, A, spos, svel, rec, start, end, O);
+    /* 16 warps per SM whatever the CTA size */
+    if (warps == 1u) k_forces_cc<1><<<sm_count() * 16u, 32, 0, s>>>(table, *single, A, spos, svel, rec, start, end, O);
+    else if (warps == 2u) k_forces_cc<2><<<sm_count() * 8u, 64, 0, s>>>(table, *single, A, spos, svel, rec, start, end, O);
+    else k_forces_cc<4><<<sm_count() * 4u, 128, 0, s>>>(table, *single, A, spos, svel, rec, start, end, O);
 }
 
 } // namespace fg

@@ -144,6 +144,7 @@ class World:
         return {"steps_per_kernel": list(cnt), "last_trial_ms": [round(x, 4) for x in ms],
                 "kernel": self.get_option("kernel"), "ctas_per_sm": self.get_option("ctas_per_sm"),
                 "digit_bits": self.get_option("digit_bits"), "one_pass_sort": self.get_option("one_pass_sort"),
+                "block_size": self.get_option("block_size"), "runs_per_cta": self.get_option("runs_per_cta"),
                 "list_cap": self.get_option("list_cap")}
 
     def launches_per_step(self):

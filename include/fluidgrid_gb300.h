@@ -214,7 +214,15 @@ int fg_world_set_graphs(fg_world *w, int on);
  *                         autotuner tries 16, 32 and 64)
  *   FG_OPT_AUTOTUNE_TILES bit mask of the tunables the autotuner varies:
  *                         1 = CTAs per SM, 2 = radix digit width, 4 = the
- *                         sort variant of FG_OPT_ONE_PASS_SORT (default 7)
+ *                         sort variant of FG_OPT_ONE_PASS_SORT, 8 = block
+ *                         size, 16 = runs per CTA (default 31)
+ *   FG_OPT_BLOCK_SIZE     kernels 0/1: threads per CTA of the density/force
+ *                         grids, 64, 128 (default) or 256; work items stay
+ *                         128 particles (two passes of a 64-thread CTA, two
+ *                         items per 256-thread CTA) and the threads per SM
+ *                         stay those of FG_OPT_CTAS_PER_SM
+ *   FG_OPT_RUNS_PER_CTA   kernel 2: bucket runs in flight per CTA (one warp
+ *                         each), 1, 2 or 4 (default)
  *   FG_OPT_ONE_PASS_SORT  1 = the fluid sort runs one kernel per digit pass
  *                         (decoupled look-back); 0 = upsweep, scan and
  *                         downsweep kernels per pass (default).  Same order
@@ -227,7 +235,7 @@ enum {
     FG_OPT_NEIGHBOR_LIST = 1, FG_OPT_TARGET_ORDER = 2, FG_OPT_ORDER_PERIOD = 3, FG_OPT_DIGIT_BITS = 4,
     FG_OPT_KERNEL = 5, FG_OPT_AUTOTUNE_PERIOD = 6, FG_OPT_AUTOTUNE_KERNELS = 7, FG_OPT_LIST_CAP = 8,
     FG_OPT_CTAS_PER_SM = 10, FG_OPT_AUTOTUNE_TILES = 11, FG_OPT_LIST_AUTOGROW = 12, FG_OPT_GRAPH_STEPS = 13,
-    FG_OPT_ONE_PASS_SORT = 14
+    FG_OPT_ONE_PASS_SORT = 14, FG_OPT_BLOCK_SIZE = 16, FG_OPT_RUNS_PER_CTA = 17
 };
 #define FG_NUM_KERNELS 3
 int fg_world_set_option(fg_world *w, int option, int value);

@@ -187,20 +187,23 @@ def test_tunables_do_not_change_results(name):
 
 @pytest.mark.parametrize("name", ["dam_break_16k", "odd_buckets"])
 def test_launch_shape_does_not_change_results(name):
-    """CTAs per SM of the density/force grids and the radix digit width change
-    no bit of the evolved state."""
+    """CTAs per SM and threads per CTA of the density/force grids and the
+    radix digit width change no bit of the evolved state."""
     spec = VARIANTS[name]
     outs = {}
-    for ctas, bits in ((0, 7), (8, 8), (64, 6), (1, 5), (3, 8), (17, 3)):
+    for ctas, bits, block in ((0, 7, 128), (8, 8, 64), (64, 6, 256), (1, 5, 64), (3, 8, 256), (17, 3, 128),
+                              (16, 7, 64), (32, 7, 256)):
         w = World([spec])
         w.set_option("autotune_period", 0)
         w.set_option("ctas_per_sm", ctas)
         w.set_option("digit_bits", bits)
+        w.set_option("block_size", block)
+        assert w.get_option("block_size") == block
         w.step(4)
         p, v = w.download()
-        outs[(ctas, bits)] = (p, v, w.read("DP"))
+        outs[(ctas, bits, block)] = (p, v, w.read("DP"))
         w.close()
-    base = outs[(0, 7)]
+    base = outs[(0, 7, 128)]
     for k, o in outs.items():
         for a, b in zip(o, base):
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), k
@@ -223,6 +226,7 @@ def test_autotuner_keeps_results_and_reports():
         w.close()
     assert st["steps_per_kernel"][1] == 12
     assert w_ctas in (16, 32, 64) and 6 <= st["digit_bits"] <= 8 and st["one_pass_sort"] in (0, 1)
+    assert st["block_size"] in (64, 128, 256)
     for a, b in zip(res[0], res[1]):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
@@ -360,6 +364,42 @@ def test_each_kernel_matches_oracle(kernel):
                        f64=True)
     assert (np.abs(g["DP"][:, 0] - d64[:, 0]) / d64[:, 0]).max() <= RTOL_RHO64
     _forces_check(spec, spec.pos, v0, g)
+
+
+def test_runs_per_cta_do_not_change_kernel2_results():
+    """Kernel 2 with 1, 2 or 4 bucket runs (warps) per CTA: the same bits."""
+    spec = VARIANTS["dam_break_16k"]
+    outs = {}
+    for runs in (1, 2, 4):
+        w = World([spec])
+        w.set_option("autotune_period", 0)
+        w.set_option("kernel", 2)
+        w.set_option("runs_per_cta", runs)
+        w.step(3)
+        outs[runs] = w.download()
+        w.close()
+    for r in (1, 2):
+        for a, b in zip(outs[r], outs[4]):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), r
+
+
+def test_autotuner_rounds_over_runs_per_cta_keep_kernel2_results():
+    """Autotuning rounds over kernel 2's runs per CTA (one real step per
+    candidate) evolve the state as an untuned run does."""
+    spec = VARIANTS["dam_break_16k"]
+    res = []
+    for period in (0, 1):
+        w = World([spec])
+        w.set_option("kernel", 2)
+        w.set_option("autotune_period", period)
+        w.set_option("autotune_tiles", 16)  # runs per CTA only
+        w.step(9)
+        w.check_finite()
+        assert w.get_option("runs_per_cta") in (1, 2, 4)
+        res.append(w.download())
+        w.close()
+    for a, b in zip(res[0], res[1]):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
 @pytest.mark.parametrize("kernel", [1, 2])
