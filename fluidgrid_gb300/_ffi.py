@@ -67,7 +67,7 @@ class fg_scene_desc(ctypes.Structure):
 class fg_server_config(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_particles", c_u32), ("max_admit_per_step", c_u32),
                 ("use_graphs", ctypes.c_int), ("grow_via_host", ctypes.c_int), ("pipeline_depth", ctypes.c_int),
-                ("reserved", ctypes.c_int)]
+                ("target_step_ms", c_f), ("head_wait_s", c_f), ("reserved", ctypes.c_int)]
 
 
 class fg_server_step_info(ctypes.Structure):
@@ -127,7 +127,7 @@ C_ABI_SYMBOLS = [
     "fg_sort_pairs_noalloc", "fg_selftest_bounded_wait", "fg_world_set_option", "fg_world_get_option", "fg_world_tuning_stats",
     "fg_world_counters", "fg_world_list_overflows", "fg_world_timed_blocks", "fg_world_diagnostics", "fg_server_config_defaults", "fg_server_create",
     "fg_server_destroy", "fg_server_submit", "fg_server_step", "fg_server_request", "fg_server_result",
-    "fg_server_stats",
+    "fg_server_stats", "fg_server_active",
     "fg_memcpy_d2h", "fg_memcpy_h2d",
     "fg_device_synchronize", "fg_last_error", "fg_version"]
 REFERENCE_SYMBOLS = [
@@ -206,6 +206,7 @@ def load():
     L.fg_server_request.argtypes = [VP, ctypes.c_uint64, P(fg_request_info)]
     L.fg_server_result.argtypes = [VP, ctypes.c_uint64, VP, VP, ctypes.c_int]
     L.fg_server_stats.argtypes = [VP, P(fg_server_stats_info)]
+    L.fg_server_active.argtypes = [VP, P(ctypes.c_uint64), c_u32, P(c_u32)]
     L.fg_memcpy_d2h.argtypes = [VP, VP, ctypes.c_size_t]
     L.fg_memcpy_h2d.argtypes = [VP, VP, ctypes.c_size_t]
     L.fg_last_error.restype = ctypes.c_char_p

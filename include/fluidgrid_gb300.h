@@ -323,8 +323,10 @@ int fg_selftest_bounded_wait(unsigned int spin_limit, unsigned int *flags);
  * counterpart; each scene's step is HeterogeneousSimulator::doTimeStep) ----
  * Requests -- a scene and a step count -- queue on the host.  Every
  * fg_server_step admits queued requests in arrival order while the resident
- * scenes' device bytes stay within hbm_budget_bytes (and their particles
- * within max_particles, if set), skipping requests that do not fit yet,
+ * scenes' device bytes stay within hbm_budget_bytes, their particles within
+ * max_particles (if set) and the predicted step time within target_step_ms
+ * (if set), skipping requests that do not fit yet; a younger request passes
+ * the oldest only if it finishes before the oldest can fit (backfilling),
  * advances every resident scene by one step in the same launches, and
  * retires scenes that reached their step count (their final state is kept
  * on the host until fg_server_result releases it).  A scene's result is the
@@ -332,7 +334,8 @@ int fg_selftest_bounded_wait(unsigned int spin_limit, unsigned int *flags);
 typedef struct fg_server fg_server;
 typedef struct fg_server_config {
     size_t hbm_budget_bytes;      /* device bytes the resident scenes may use */
-    uint32_t max_particles;       /* particles advanced per step, 0 = no limit */
+    uint32_t max_particles;       /* particles advanced per step, 0 = no limit (default 850,000;
+                                     a larger scene is refused with FG_E_BUDGET) */
     uint32_t max_admit_per_step;  /* 0 = no limit */
     int use_graphs;               /* replay captured steps while the resident set is stable */
     int grow_via_host;            /* 1: when the world grows, always park the state on the host
@@ -340,6 +343,15 @@ typedef struct fg_server_config {
     int pipeline_depth;           /* steps fg_server_step may leave running on the device (0 =
                                      return after each step finishes); a change of the resident
                                      set, a retirement or a result waits for all of them */
+    float target_step_ms;         /* per-step work budget: a request is admitted only while the
+                                     predicted device time of one step over the resident scenes
+                                     stays within it (an empty server admits any request); the
+                                     prediction is a fixed 0.1 ms plus a per-particle rate learned
+                                     from the finished steps; 0 = no time budget (default 0.9) */
+    float head_wait_s;            /* once the oldest queued request has waited this long and does
+                                     not fit, it gets a reservation: a younger request is admitted
+                                     only if it fits now and finishes before enough resident scenes
+                                     have left for the oldest to fit (backfilling); default 0 */
     int reserved;
 } fg_server_config;
 enum { FG_REQ_QUEUED = 0, FG_REQ_ACTIVE = 1, FG_REQ_DONE = 2 };
@@ -368,7 +380,8 @@ typedef struct fg_server_stats_info {
     uint64_t resident_particles;
     size_t device_bytes;      /* bytes the server's world holds (capacity) */
 } fg_server_stats_info;
-void fg_server_config_defaults(fg_server_config *cfg); /* 120 GiB budget, graphs on */
+/* 120 GiB budget, graphs on, 850k particles and a predicted 0.9 ms per step */
+void fg_server_config_defaults(fg_server_config *cfg);
 int fg_server_create(const fg_server_config *cfg, fg_stream_t stream, fg_server **out);
 void fg_server_destroy(fg_server *s);
 /* Copies the description and its arrays.  FG_E_BUDGET if the scene alone
@@ -381,6 +394,9 @@ int fg_server_request(const fg_server *s, uint64_t request_id, fg_request_info *
  * not finished. */
 int fg_server_result(fg_server *s, uint64_t request_id, float *pos4, float *vel4, int release);
 int fg_server_stats(const fg_server *s, fg_server_stats_info *stats);
+/* Request ids of the resident scenes (the ones the next step advances), at
+ * most `cap` of them; *count receives how many are resident. */
+int fg_server_active(const fg_server *s, uint64_t *ids, uint32_t cap, uint32_t *count);
 
 /* Small helpers so callers without a CUDA runtime binding can move data. */
 int fg_memcpy_d2h(void *dst, const void *src, size_t bytes);

@@ -54,8 +54,9 @@ int main(void) {
   printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(fg_scene_desc), offsetof(fg_scene_desc, bodies),
          offsetof(fg_scene_desc, rb_volume_max), sizeof(fg_body_desc), offsetof(fg_body_desc, inv_inertia),
          sizeof(fgr_common_fluid_params), offsetof(fgr_common_fluid_params, fluid_to_srb_relation));
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(fg_server_config),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(fg_server_config),
          offsetof(fg_server_config, use_graphs), offsetof(fg_server_config, pipeline_depth),
+         offsetof(fg_server_config, target_step_ms), offsetof(fg_server_config, head_wait_s),
          sizeof(fg_server_step_info),
          offsetof(fg_server_step_info, wall_ms), offsetof(fg_server_step_info, resident_bytes),
          sizeof(fg_request_info), offsetof(fg_request_info, submit_s), offsetof(fg_request_info, resident_bytes),
@@ -80,7 +81,8 @@ def test_struct_layouts_match_ctypes():
             ctypes.sizeof(C), C.fluid_to_srb_relation.offset]
     SC, SI, RI, ST = (_ffi.fg_server_config, _ffi.fg_server_step_info, _ffi.fg_request_info,
                       _ffi.fg_server_stats_info)
-    want += [ctypes.sizeof(SC), SC.use_graphs.offset, SC.pipeline_depth.offset, ctypes.sizeof(SI), SI.wall_ms.offset,
+    want += [ctypes.sizeof(SC), SC.use_graphs.offset, SC.pipeline_depth.offset, SC.target_step_ms.offset,
+             SC.head_wait_s.offset, ctypes.sizeof(SI), SI.wall_ms.offset,
              SI.resident_bytes.offset, ctypes.sizeof(RI), RI.submit_s.offset, RI.resident_bytes.offset,
              ctypes.sizeof(ST), ST.device_bytes.offset]
     assert got == want
@@ -185,3 +187,14 @@ def test_run_stage_codes_match_header():
     assert contact == _ffi.RUN_WITH_CONTACT
     # the stages are numbered in step order, from 1
     assert sorted(run.values()) == list(range(1, len(run) + 1))
+
+
+def test_server_config_defaults(lib):
+    """The served form admits by HBM budget and by a per-step work budget
+    (particles and predicted time), with reservations for the oldest
+    request."""
+    c = _ffi.fg_server_config()
+    lib.fg_server_config_defaults(ctypes.byref(c))
+    assert c.hbm_budget_bytes == 120 << 30 and c.use_graphs == 1
+    assert c.max_particles == 850000 and c.target_step_ms == pytest.approx(0.9)
+    assert c.head_wait_s == 0.0 and c.pipeline_depth == 0

@@ -107,3 +107,77 @@ def test_particle_limit_queues_requests():
         st = srv.stats()
         assert st["queued"] == 0 and st["active"] == 0 and st["resident_bytes"] == 0
         assert st["particle_steps"] == sum(s.n * n for s, n in zip(ss, steps))
+
+
+def _blocks(sizes, seed=5):
+    rng = np.random.default_rng(seed)
+    return [scenes.dam_break_request(n, 0, rng, name="block_%d" % k) for k, n in enumerate(sizes)]
+
+
+def test_time_budget_bounds_the_resident_particles():
+    """With a per-step time budget the server admits only as many particles
+    as its learned rate says fit one step in the budget; without one it
+    admits everything that fits the other budgets at once.  Results stay the
+    scene alone's bits."""
+    ss = _blocks([65536] * 8)
+    steps = [6] * 8
+    total = sum(s.n for s in ss)
+    with Server(target_step_ms=0, max_particles=0) as free:
+        ids = [free.submit(s, n) for s, n in zip(ss, steps)]
+        info = free.step()
+        assert info["active_particles"] == total
+        while not all(free.done(i) for i in ids):
+            free.step()
+    with Server(target_step_ms=0.12, max_particles=0) as srv:
+        ids = [srv.submit(s, n) for s, n in zip(ss, steps)]
+        most = 0
+        while not all(srv.done(i) for i in ids):
+            info = srv.step()
+            most = max(most, info["active_particles"])
+        # predicted 0.1 ms + 0.9 ns per particle: one scene fits 0.12 ms, two
+        # do not, and steps of fewer than 100k particles teach no new rate
+        assert most == 65536
+        for k in (0, 7):
+            p, v = srv.result(ids[k])
+            pa, va = _alone(ss[k], steps[k])
+            assert np.array_equal(p.view(np.uint32), pa.view(np.uint32)), k
+
+
+def test_reservation_backfills_only_requests_done_in_time():
+    """When the oldest request does not fit it gets a reservation: a younger
+    request passes it only if it is done before the oldest can fit
+    (backfilling).  Without reservations (head_wait_s beyond the run) any
+    younger request that fits passes it."""
+    ss = _blocks([12000, 15000, 2000, 2000])
+    steps = [4, 3, 3, 10]  # A runs 4 steps; C (3 steps) can finish before B fits, D (10) cannot
+    order = {}
+    for wait in (0.0, 1e9):
+        with Server(max_particles=20000, target_step_ms=0, head_wait_s=wait) as srv:
+            ids = [srv.submit(s, n) for s, n in zip(ss, steps)]
+            while not all(srv.done(i) for i in ids):
+                srv.step()
+            order[wait] = [srv.request(i)["admit_s"] for i in ids]
+            for k in range(4):
+                p, v = srv.result(ids[k])
+                pa, _ = _alone(ss[k], steps[k])
+                assert np.array_equal(p.view(np.uint32), pa.view(np.uint32)), k
+    a, b, c, d = order[0.0]
+    assert c < b          # C is backfilled: it is done before B fits
+    assert b <= d         # D would still be running: it waits behind B
+    a, b, c, d = order[1e9]
+    assert d < b          # no reservation: D passes B
+
+
+def test_active_lists_the_resident_requests():
+    ss = _blocks([3000, 4000, 5000])
+    with Server() as srv:
+        ids = [srv.submit(s, n) for s, n in zip(ss, (2, 4, 6))]
+        assert srv.active() == []
+        srv.step()
+        assert sorted(srv.active()) == sorted(ids)
+        srv.step()
+        srv.step()
+        assert sorted(srv.active()) == sorted(ids[1:])
+        while not all(srv.done(i) for i in ids):
+            srv.step()
+        assert srv.active() == []
