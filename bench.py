@@ -157,9 +157,40 @@ def profile_value(key, kernel):
     return None
 
 
-def profile_traffic(kernel):
-    """DRAM bytes per particle of `kernel` (ncu, dense phase), or None."""
-    return profile_value("traffic_bytes_per_particle", kernel)
+def profile_traffic(kernel, phase):
+    """DRAM bytes per particle of `kernel` in the trajectory phase `phase`
+    ("sparse": the opening steps, "dense": the compressed middle) from the
+    committed ncu summary, or None."""
+    return profile_value("traffic_bytes_per_particle_" + phase, kernel)
+
+
+def window_phase(first_step, last_step):
+    """The trajectory phase a timed window of the 1M dam break lies in: the
+    block stays near its lattice density for the first ~60 steps and then
+    compresses (in-range neighbours ~29 -> ~110 by step ~150)."""
+    mid = 0.5 * (first_step + last_step)
+    return "sparse" if mid <= 60 else "dense"
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu or /proc/cpuinfo), or None."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.split(":")[0].strip() in ("Model name", "Model"):
+                v = ln.split(":", 1)[1].strip()
+                if v and not v.isdigit():
+                    return v
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith(("model name", "cpu part", "hardware")):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return None
 
 
 def make_scene(name):
@@ -181,8 +212,59 @@ def cpu_baseline(spec, budget_s=15.0, max_steps=60):
         done += 1
     dt = time.perf_counter() - t0
     return {"value": spec.n * done / dt, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "cpu_model": cpu_model(),
             "sample": "%d full steps of %s (%d particles, %d rigid spheres) in %.1f s" % (
                 done, spec.name, spec.n, spec.nspheres, dt), "pairs_per_step": st.pairs}
+
+
+def parity_of_step(spec, state):
+    """Errors of one GPU step of the benched scene against the FP64 oracle
+    from the identical state (the oracle is the checker here): grid order and
+    ranges, density relative to FP64, fluid force per particle relative to
+    max(|F64|, median |F64|) with the rigid contact term, and the FP64 body
+    force sums.  `state` holds the GPU's state before the step and its
+    buffers after it."""
+    from oracle import oracle as O
+    pos0, v0, before, g = state["pos0"], state["vel0"], state["before"], state["after"]
+    p = O.make_common_params(spec.cell_size, spec.buckets, spec.h, spec.vlimit, spec.box_min, spec.box_max,
+                             spec.gravity, spec.scale, spec.dt, relation=spec.f2r_rel, point_radius=spec.fluid_radius)
+    keys, ids = O.calc_hash_key(pos0, spec.nbuckets, spec.cell_size)
+    sk, si = O.sort_pairs(keys, ids)
+    start, end, spos, svel = O.find_cell_offset(sk, si, pos0, v0, spec.nbuckets)
+    grid_exact = bool(np.array_equal(g["IDS"], si) and np.array_equal(g["START"], start))
+    kc = O.kernels_cache(spec.h)
+    d64, pairs = O.density(spos, start, end, p, kc, spec.gas, spec.rest, spec.mass, f64=True)
+    act = spos[:, 3] > 0
+    e_rho = np.abs(g["DP"][act, 0].astype(np.float64) - d64[act, 0]) / d64[act, 0]
+    contact = None
+    out = {}
+    if spec.bodies:
+        nb_r = int(np.prod(spec.rb_buckets))
+        cell = (spec.rb_radius,) * 3
+        rk, ri, rw = O.calc_hash_key_with_offset(before["RB_LOCAL"], before["BODY_XF"], before["BODY_QF"], nb_r, cell)
+        rsk, rsi = O.sort_pairs(rk, ri)
+        rst, ren, rsp, _ = O.find_cell_offset(rsk, rsi, rw, None, nb_r)
+        F64, _ = O.rb_forces_from_fluids(rsp, before["BODY_VF"], before["BODY_XF"], spec.rb_radius, spos, svel, start,
+                                         end, spec.fluid_radius, spec.cell_size, spec.nbuckets, spec.r2f_rel, spec.ck,
+                                         spec.ckd, f64=True)
+        bf = np.zeros((len(spec.bodies), 3))
+        np.add.at(bf, F64[:, 3].astype(np.int64), F64[:, :3])
+        scale_f = max(np.abs(bf).max(), 1e-30)
+        out["body_force_rel_max_vs_fp64"] = float((np.abs(g["BODY_FSUM"][:, :3] - bf) /
+                                                   np.maximum(np.abs(bf), 1e-3 * scale_f)).max())
+        cp = O.contact_params(spec.fluid_radius, spec.rb_radius, spec.ck, spec.ckd, cell, spec.f2r_rel, 0.003)
+        contact = (cp, None, O.contact_grid(rsp, before["BODY_VF"], rst, ren, nb_r))
+    nv64 = O.forces(spos, svel, d64.astype(np.float32), start, end, si, spec.mass, spec.visc, p, kc, f64=True,
+                    newvel_init=v0, contact=contact)
+    Fg = (g["VEL"][:, :3].astype(np.float64) - v0[:, :3]) / spec.dt
+    Fr = (nv64[:, :3] - v0[:, :3].astype(np.float64)) / spec.dt
+    mag = np.linalg.norm(Fr, axis=1)
+    e_f = (np.linalg.norm(Fg - Fr, axis=1) / np.maximum(mag, np.median(mag)))[pos0[:, 3] > 0]
+    out.update({"step": state["step"], "grid_bit_exact": grid_exact,
+                "density_rel_max_vs_fp64": float(e_rho.max()), "force_rel_max_vs_fp64": float(e_f.max()),
+                "pairs_per_particle": float(pairs) / len(pos0),
+                "bars": {"density": 1e-5, "force": 2e-4, "body_force": 1e-4}})
+    return out
 
 
 def run_reference(args, rank, world):
@@ -214,6 +296,7 @@ def run_reference(args, rank, world):
             "config": {"workload": spec.name, "particles": spec.n, "buckets": spec.nbuckets,
                        "rigid_spheres": spec.nspheres, "bodies": len(spec.bodies)},
             "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": O.max_threads(), "kind": "port",
+                             "cpu_model": cpu_model(),
                              "sample": "%d timed full steps (of %d requested, %.0f s budget) after %d warm-up "
                                        "steps" % (done, args.steps, REF_BUDGET_S, args.warmup)},
             "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -269,15 +352,29 @@ def run_batched(steps=1000, warmup=10, plain_sample=64):
             "autotune": tuning}
 
 
-def run_served(duration=20.0, rate=200.0, budget=120 << 30, max_particles=0, seed=0x5EED, label="served",
-               pipeline_depth=2):
-    """Served form: Poisson arrivals of dam-break requests (fluid counts
-    log-uniform in [4,096, 524,288], 0-4 rigid boxes of 1,024 spheres, step
-    counts uniform in [100, 2000]) for `duration` seconds of wall time into a
-    continuous-batching server with an HBM budget; every server step admits
-    what fits and advances every resident scene, leaving up to
-    `pipeline_depth` steps running while the host prepares the next."""
-    from fluidgrid_gb300 import scenes
+SIZE_CLASSES = (("<=65536", 0, 65536), ("65537-262144", 65537, 262144), (">262144", 262145, 1 << 40))
+
+
+def size_class(n):
+    for name, lo, hi in SIZE_CLASSES:
+        if lo <= n <= hi:
+            return name
+    return SIZE_CLASSES[-1][0]
+
+
+def run_served(duration=60.0, rate=200.0, budget=120 << 30, seed=0x5EED, pipeline_depth=2):
+    """Served form (the C5 workload): Poisson arrivals at `rate` per second of
+    dam-break requests (fluid counts log-uniform in [4,096, 524,288], 0-4
+    rigid boxes of 1,024 spheres, step counts uniform in [100, 2000]) for
+    `duration` seconds of wall time into a continuous-batching server with
+    its default admission policy: the HBM budget, a per-step work budget that
+    bounds every resident scene's step latency, and reservations with
+    backfilling for the oldest request.  Every server step advances every
+    resident scene; up to `pipeline_depth` steps stay in flight while the
+    host prepares the next.  Step latency is recorded for every resident
+    scene and reported per size class."""
+    import ctypes
+    from fluidgrid_gb300 import _ffi, scenes
     from fluidgrid_gb300.server import Server
     pool = scenes.served_templates(seed=seed)
     rng = np.random.default_rng(seed + 1)
@@ -285,9 +382,14 @@ def run_served(duration=20.0, rate=200.0, budget=120 << 30, max_particles=0, see
     arrivals = arrivals[arrivals < duration]
     picks = rng.integers(0, len(pool), len(arrivals))
     nsteps = rng.integers(100, 2001, len(arrivals))
-    srv = Server(budget_bytes=budget, max_particles=max_particles, pipeline_depth=pipeline_depth)
+    cfg = _ffi.fg_server_config()
+    _ffi.load().fg_server_config_defaults(ctypes.byref(cfg))
+    policy = {"hbm_budget_bytes": budget, "max_particles_per_step": int(cfg.max_particles),
+              "target_step_ms": round(float(cfg.target_step_ms), 3), "head_wait_s": round(float(cfg.head_wait_s), 3)}
+    srv = Server(budget_bytes=budget, pipeline_depth=pipeline_depth)
     ids = []
     infos = []
+    by_class = {name: [] for name, _, _ in SIZE_CLASSES}
     t0 = time.perf_counter()
     k = 0
     while True:
@@ -297,29 +399,52 @@ def run_served(duration=20.0, rate=200.0, budget=120 << 30, max_particles=0, see
         while k < len(arrivals) and arrivals[k] <= now:
             ids.append(srv.submit(pool[picks[k]], int(nsteps[k])))
             k += 1
-        infos.append(srv.step())
+        resident = srv.active()
+        info = srv.step()
+        infos.append(info)
+        if info["step_ms"] > 0:
+            for cls in {size_class(srv.n_of[r]) for r in resident}:
+                by_class[cls].append(info["step_ms"])
     elapsed = time.perf_counter() - t0
     st = srv.stats()
-    reqs = [srv.request(i) for i in ids]
+    reqs = [(srv.request(i), srv.n_of[i]) for i in ids]
     srv.close()
-    done = [r for r in reqs if r["state"] == 2]
-    admitted = [r for r in reqs if r["state"] >= 1]
-    step_ms = [i["step_ms"] for i in infos if i["active_particles"]]
+    done = [(r, n) for r, n in reqs if r["state"] == 2]
+    admitted = [(r, n) for r, n in reqs if r["state"] >= 1]
+    step_ms = [i["step_ms"] for i in infos if i["active_particles"] and i["step_ms"] > 0]
     wall_ms = [i["wall_ms"] for i in infos if i["active_particles"]]
-    return {"workload": label, "duration_s": duration, "arrival_rate_per_s": rate, "budget_bytes": budget,
-            "max_particles_per_step": max_particles, "pipeline_depth": pipeline_depth,
-            "submitted": len(ids), "admitted": len(admitted),
+    lat_cls = {}
+    for name, _, _ in SIZE_CLASSES:
+        d = by_class[name]
+        rl = [r["done_s"] - r["submit_s"] for r, n in done if size_class(n) == name]
+        lat_cls[name] = {"step_samples": len(d), "p50": pct(d, 50), "p99": pct(d, 99),
+                         "completed": len(rl), "request_latency_s_p50": pct(rl, 50),
+                         "request_latency_s_p99": pct(rl, 99)}
+    return {"workload": "served_c5", "duration_s": duration, "arrival_rate_per_s": rate, "policy": policy,
+            "pipeline_depth": pipeline_depth, "submitted": len(ids), "admitted": len(admitted),
             "completed": len(done), "queued_at_end": st["queued"], "server_steps": st["steps"],
             "value": st["particle_steps"] / elapsed, "unit": "particle-steps/s",
             "step_latency_ms": {"p50": pct(step_ms, 50), "p99": pct(step_ms, 99)},
+            "step_latency_ms_by_size_class": lat_cls,
             "server_step_wall_ms": {"p50": pct(wall_ms, 50), "p99": pct(wall_ms, 99)},
-            "request_latency_s": {"p50": pct([r["done_s"] - r["submit_s"] for r in done], 50),
-                                  "p99": pct([r["done_s"] - r["submit_s"] for r in done], 99)},
-            "admission_wait_s": {"p50": pct([r["admit_s"] - r["submit_s"] for r in admitted], 50),
-                                 "p99": pct([r["admit_s"] - r["submit_s"] for r in admitted], 99)},
+            "request_latency_s": {"p50": pct([r["done_s"] - r["submit_s"] for r, _ in done], 50),
+                                  "p99": pct([r["done_s"] - r["submit_s"] for r, _ in done], 99)},
+            "admission_wait_s": {"p50": pct([r["admit_s"] - r["submit_s"] for r, _ in admitted], 50),
+                                 "p99": pct([r["admit_s"] - r["submit_s"] for r, _ in admitted], 99)},
             "max_resident_particles": int(max([i["active_particles"] for i in infos] + [0])),
             "max_resident_bytes": int(max([i["resident_bytes"] for i in infos] + [0])),
-            "device_bytes": st["device_bytes"]}
+            "device_bytes": st["device_bytes"],
+            "note": "arrivals ask ~2e10 particle-steps/s, ~20x the GPU: the queue grows and the admission "
+                    "policy decides what runs"}
+
+
+TRAJECTORY_STEPS = 500  # the configured dam-break trajectory (3 warm-up + 497 timed)
+STATE_NAMES = ("RB_LOCAL", "BODY_X", "BODY_V", "BODY_Q", "BODY_L", "BODY_XF", "BODY_VF", "BODY_QF")
+AFTER_NAMES = ("IDS", "START", "DP", "VEL", "BODY_FSUM")
+
+
+def stage_means(prof):
+    return {key: float(np.mean([p[key] for p in prof])) for key in prof[0]} if prof else {}
 
 
 def run_ours(args, rank, world, local):
@@ -351,10 +476,18 @@ def run_ours(args, rank, world, local):
     w.check_finite()
     tuning = w.tuning_stats()
     tuning["list_overflow_particle_steps"] = w.list_overflows(reset=True)
+    # the state at the end of the window and one more step from it: the
+    # parity check's input (compared with the oracle in the CPU-baseline leg)
+    pstate = None
+    if rank == 0 and not args.no_cpu_baseline:
+        pos0, vel0 = w.download()
+        before = {k: w.read(k) for k in STATE_NAMES} if spec.bodies else {}
+        w.step(1)
+        pstate = {"step": W + K + 1, "pos0": pos0, "vel0": vel0, "before": before,
+                  "after": {k: w.read(k) for k in AFTER_NAMES}}
     w.close()
-    # 2. end to end on the same trajectory: every step uploads the particle
-    #    state from pinned host memory and downloads it again (the download of
-    #    step k is the upload of step k+1)
+    # 2. end to end on the same window: every step uploads the particle state
+    #    from pinned host memory and downloads it again
     w = World([spec])
     w.step(W)
     pos, vel = w.download()
@@ -368,42 +501,69 @@ def run_ours(args, rank, world, local):
     hp.free()
     hv.free()
     w.close()
-    # 3. per-stage breakdown along the same trajectory (every 25th step)
+    # 3. per-stage breakdown over the same window (about 20 profiled steps)
+    every = max(1, K // 20)
     w = World([spec])
     w.step(W)
     prof = []
     for k in range(K):
-        if k % 25 == 12:
+        if k % every == every // 2:
             prof.append(w.stage_profile(FLUSH_BYTES))
         else:
             w.step(1)
     w.close()
-    stages = {key: float(np.mean([p[key] for p in prof])) for key in prof[0]} if prof else {}
+    stages = stage_means(prof)
+    # 4. the whole configured trajectory, unless the window already is it
+    traj = None
+    if W + K < TRAJECTORY_STEPS:
+        w = World([spec])
+        w.step(3)
+        tms = w.timed_steps(TRAJECTORY_STEPS - 3, FLUSH_BYTES)
+        w.close()
+        w = World([spec])
+        tprof = []
+        for k in range(TRAJECTORY_STEPS):
+            if k % 25 == 12:
+                tprof.append(w.stage_profile(FLUSH_BYTES))
+            else:
+                w.step(1)
+        w.close()
+        traj = {"steps": TRAJECTORY_STEPS - 3, "warmup": 3, "ms_per_step": float(tms.mean()),
+                "value": world * n / (float(tms.mean()) * 1e-3), "unit": "particle-steps/s",
+                "step_ms": {"p50": pct(tms, 50), "p99": pct(tms, 99)}, "stages_ms": stage_means(tprof)}
     value = world * n * K / (total_ms * 1e-3)
     e2e_value = world * n * K / (e2e_ms * 1e-3)
-    # 4. the batched and served forms (one GPU each rank, replicas)
+    # 5. the batched and served forms (one GPU each rank, replicas)
     forms = {}
     if "batched" in args.forms:
         forms["batched"] = run_batched()
     if "served" in args.forms:
         forms["served"] = run_served(duration=args.served_seconds)
-        # latency-bounded serving: at most 750k particles advanced per step
-        forms["served_latency"] = run_served(duration=args.served_seconds / 2, max_particles=750_000,
-                                             label="served_latency_bounded")
     if rank == 0:
         peak, peak_kind = measured_peaks()
+        phase = window_phase(W, W + K)
+
+        def hbm(kernel, stage, per_p):
+            a = per_p * n / (stages[stage] * 1e-3) / 1e9
+            t = profile_traffic(kernel, phase)
+            return {"kernel": kernel, "achieved": a, "peak": peak, "unit": "GB/s", "frac": a / peak,
+                    "bytes_per_particle": per_p, "traffic": (t * n) if t else None, "traffic_phase": phase,
+                    "ms": stages[stage]}
         dom = max(("forces", "density"), key=lambda k: stages.get(k, 0.0))
-        per_p = BYTES_FORCES if dom == "forces" else BYTES_DENSITY
-        achieved = per_p * n / (stages[dom] * 1e-3) / 1e9
         dom_kernel = "k_forces" if dom == "forces" else "k_density"
-        tpp = profile_traffic(dom_kernel)
+        roof = hbm(dom_kernel, dom, BYTES_FORCES if dom == "forces" else BYTES_DENSITY)
         cpu = None if args.no_cpu_baseline else cpu_baseline(spec)
         fp32_peak = fp32_peak_tflops()
         pairs_per_step = pair_visits / max(counted, 1)
         flops = (FLOPS_FORCE_PAIR * (pairs_per_step - n)) if dom == "forces" else FLOPS_DENSITY_PAIR * pairs_per_step
         ach = flops / (stages[dom] * 1e-3) / 1e12
-        fp32 = {"achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
-                "pairs_per_step": pairs_per_step, "peak_kind": "measured (FMA probe)"}
+        roof.update({"bound": "hbm", "peak_kind": peak_kind,
+                     "issue_active_pct": profile_value("issue_active_pct_" + phase, dom_kernel),
+                     "fp32": {"achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
+                              "pairs_per_step": pairs_per_step, "peak_kind": "measured (FMA probe)"},
+                     "force_kernel": hbm("k_forces", "forces", BYTES_FORCES),
+                     "density_kernel": hbm("k_density", "density", BYTES_DENSITY)})
+        parity = parity_of_step(spec, pstate) if pstate is not None else None
         ms_sorted = np.sort(ms)
         line = {
             "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
@@ -412,19 +572,17 @@ def run_ours(args, rank, world, local):
             "data": "synthetic (seeded jittered lattice + rigid box, seed 0x5EED)",
             "config": {"workload": spec.name, "particles": n, "buckets": spec.nbuckets,
                        "rigid_spheres": spec.nspheres, "bodies": len(spec.bodies),
-                       "trajectory_steps": W + K,
+                       "trajectory_steps": [W, W + K], "trajectory_phase": phase,
                        "l2": "flushed before every timed step (256 MiB write)",
                        "parallelism": "replicas" if world > 1 else "single",
                        "autotune": tuning},
             "latency_ms": {"p50": float(np.percentile(ms_sorted, 50)), "p99": float(np.percentile(ms_sorted, 99)),
                            "max": float(ms_sorted[-1]), "slowest_steps": [int(W + k) for k in np.argsort(-ms)[:5]]},
             "stages_ms": stages,
-            "roofline": {"bound": "hbm", "kernel": dom_kernel,
-                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": (tpp * n) if tpp else None, "peak_kind": peak_kind,
-                         "issue_active_pct": profile_value("issue_active_pct", dom_kernel),
-                         "bytes_per_particle": per_p, "fp32": fp32},
+            "trajectory_mean": traj,
+            "roofline": roof,
             "cpu_baseline": ({k: v for k, v in cpu.items() if k != "pairs_per_step"} if cpu else None),
+            "parity": parity,
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": 32 * n,
                     "d2h_bytes_per_step": 32 * n, "ms_per_step": e2e_ms / K,
                     "step_ms": {"p50": float(np.percentile(ems, 50)), "p99": float(np.percentile(ems, 99)),
@@ -449,7 +607,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--forms", default="batched,served",
                     help="comma list of extra forms to measure after the plain path: batched, served")
-    ap.add_argument("--served-seconds", type=float, default=20.0)
+    ap.add_argument("--served-seconds", type=float, default=60.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
