@@ -76,12 +76,22 @@ __device__ __forceinline__ void fg_ld_rec(const float4 *p, float4 &a, float4 &b)
 }
 
 /* Eight list entries (one 32-byte sector) in a single 256-bit load of
- * read-only data; p must be 32-byte aligned. */
+ * read-only data; p must be 32-byte aligned.  A list is read once: the load
+ * skips L1 and marks its L2 lines evict-first, so the lists stream past the
+ * particle records instead of pushing them out of L2. */
 __device__ __forceinline__ void fg_ld_idx8(const uint32_t *p, uint4 &a, uint4 &b)
 {
-    asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+    asm("ld.global.nc.L1::no_allocate.L2::evict_first.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
         : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w), "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w)
         : "l"(p));
+}
+
+/* Two list entries stored with the streaming (evict-first) policy: a list
+ * is written once by the density pass and read once by the force pass. */
+__device__ __forceinline__ void fg_st_list2(uint32_t *p, uint32_t a, uint32_t b)
+{
+    /* no memory clobber: no kernel reads a list it writes */
+    asm volatile("st.global.cs.v2.b32 [%0], {%1, %2};" ::"l"(p), "r"(a), "r"(b));
 }
 
 /* select one of three register values without local-memory indexing */

@@ -101,7 +101,7 @@ struct DensityAcc {
                 q2 = q3;
                 q3 = j;
                 cnt++;
-                if ((cnt & 1u) == 0u && cnt <= cap) *reinterpret_cast<uint2 *>(lp + cnt - 2u) = make_uint2(q2, q3);
+                if ((cnt & 1u) == 0u && cnt <= cap) fg_st_list2(lp + cnt - 2u, q2, q3);
             }
         }
     }
@@ -114,12 +114,12 @@ struct DensityAcc {
         if (cnt > cap) return;
         const uint32_t r = cnt & 3u;
         if (r == 1u) {
-            *reinterpret_cast<uint2 *>(lp + cnt - 1u) = make_uint2(q3, self);
-            *reinterpret_cast<uint2 *>(lp + cnt + 1u) = make_uint2(self, self);
+            fg_st_list2(lp + cnt - 1u, q3, self);
+            fg_st_list2(lp + cnt + 1u, self, self);
         } else if (r == 2u) {
-            *reinterpret_cast<uint2 *>(lp + cnt) = make_uint2(self, self);
+            fg_st_list2(lp + cnt, self, self);
         } else if (r == 3u) {
-            *reinterpret_cast<uint2 *>(lp + cnt - 1u) = make_uint2(q3, self);
+            fg_st_list2(lp + cnt - 1u, q3, self);
         }
     }
 };
