@@ -14,12 +14,18 @@
  * neighbour-inclusion tests (so the neighbour sets are identical) and carry
  * every accumulated quantity in double.
  *
- * Parity of the restated helpers (HashKeyD, wall forces, collision forces,
- * quaternion math) is pinned against the reference's own helper source files
- * compiled on the host (oracle/ref_wrap.cpp -> golden vectors in tests/golden).
- * The __global__ loops of the reference cannot be compiled by any current
- * toolchain (texture references were removed in CUDA 12), so their loop
- * structure is restated here and pinned only through the helpers.
+ * Pinning, both bit for bit against golden vectors in tests/golden:
+ *   - the restated helpers (HashKeyD, wall forces, collision forces,
+ *     quaternion math) against the reference's own helper source files
+ *     compiled on the host (oracle/ref_wrap.cpp, ref_helpers.npz);
+ *   - the restated kernels (density, forces with and without the rigid
+ *     grids, integration, hashing, cell ranges, rigid contact and rigid
+ *     integration) against the reference's own __global__ kernels run on the
+ *     host (oracle/ref_kernels_*.cpp over the kernel sections of
+ *     K_FluidSim.cu, K_HashGrid.cu and K_RigidBodySim.cu, ref_kernels.npz).
+ * Library math the source calls (powf, sqrtf) is the host C library's on both
+ * sides; sqrtf is exact, and the GPU's own powf may differ from the host's in
+ * the last bit.
  */
 #include <cmath>
 #include <cstdint>
@@ -540,7 +546,8 @@ static void density_impl(const float *spos4, R *dp2, const u32 *start, const u32
                             if (l < h) {
                                 pairs++;
                                 if (sizeof(R) == 4) {
-                                    part += (R)((mass * kc->kPoly6) * (float)std::pow((double)(h2 - (l * l)), 3.0));
+                                    /* powf as the source calls it (the host C library's) */
+                                    part += (R)((mass * kc->kPoly6) * powf(h2 - (l * l), 3.0f));
                                 } else {
                                     V3<R> d = mk3<R>((R)P.x * scale - (R)q.x * scale, (R)P.y * scale - (R)q.y * scale,
                                                      (R)P.z * scale - (R)q.z * scale);
