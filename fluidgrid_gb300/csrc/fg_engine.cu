@@ -388,6 +388,13 @@ int World::set_layout(const fg_scene_desc *d, uint32_t ns)
     for (uint32_t s = 0; s < ns; s++)
         if (scenes_h[s].nsph > FG_RB_SCENE_MAX) rb_small_scenes = false;
     total_buckets = (uint32_t)nbk;
+    /* the counting sort's work grows with the buckets, the radix sort's
+     * with the particles and passes */
+    if (!sort_chosen)
+        set_sort_variant((total_buckets <= (uint64_t)FG_BUCKET_SORT_RATIO * std::max<uint32_t>(n, 1u) &&
+                          bucket_sort_fits())
+                             ? 2
+                             : (one_pass_sort ? 1 : 0));
     nspheres = (uint32_t)nsph;
     nbodies = (uint32_t)nbod;
     total_rb_buckets = (uint32_t)nrbk;
@@ -654,6 +661,23 @@ void World::enqueue_bodies(cudaStream_t st, float4 *vf)
                        rb_force, rb_torque, b, 1, st);
 }
 
+/* The fluid sort of the variant in use: keys_u -> keys, ids (and, for the
+ * counting sort, start/end). */
+void World::enqueue_sort()
+{
+    if (bucket_sort_on &&
+        bucket_sort(keys_u, keys, ids, n, total_buckets, start, end, rs,
+                    (uint32_t)std::min<size_t>(radix_hist_words((uint32_t)std::max<uint64_t>(cap.particles, 1)),
+                                               0xffffffffu),
+                    stream)) {
+        counted_ranges = true;
+        return;
+    }
+    if (one_pass_sort && onesweep_sort(keys_u, keys, ids, n, key_bits, digit_bits, rs, os_scratch, status_d, stream))
+        return;
+    radix_sort(keys_u, nullptr, keys, ids, n, key_bits, digit_bits, rs, stream);
+}
+
 uint32_t World::enqueue_step(cudaEvent_t *ev)
 {
     /* ev: optional 16 events, (2k, 2k+1) bracket stage bit k */
@@ -693,21 +717,18 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         mark(0, 1);
         launches++;
     }
+    counted_ranges = false;
     if (stages & FG_STAGE_SORT) {
         mark(1, 0);
-        if (one_pass_sort && onesweep_sort(keys_u, keys, ids, n, key_bits, digit_bits, rs, os_scratch, status_d,
-                                           stream)) {
-            launches += 2 + radix_passes(key_bits, digit_bits);
-        } else {
-            radix_sort(keys_u, nullptr, keys, ids, n, key_bits, digit_bits, rs, stream);
-            launches += 3 * radix_passes(key_bits, digit_bits);
-        }
+        enqueue_sort();
+        launches += sort_launches();
         mark(1, 1);
     }
     if (cur_io && iob) CK0(cudaStreamWaitEvent(stream, ev_vel_in, 0));
     if (stages & FG_STAGE_RANGES) {
         mark(2, 0);
-        cudaMemsetAsync(start, 0xff, 4 * (size_t)total_buckets, stream);
+        /* the counting sort wrote start[] of every bucket already */
+        if (!counted_ranges) cudaMemsetAsync(start, 0xff, 4 * (size_t)total_buckets, stream);
         if (needs_runs()) {
             cudaMemsetAsync(nruns, 0, 4, stream);
             launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv, runs, nruns);
@@ -812,7 +833,7 @@ uint64_t World::graph_signature() const
     return (uint64_t)((stages & 0xffu) | (fused_integrate ? 0x100u : 0u) | (digit_bits << 9) |
                       (use_list ? 0x10000u : 0u) | ((use_order && order_valid) ? 0x20000u : 0u) |
                       (use_cc ? 0x40000u : 0u) | ((ctas_per_sm & 0x7fu) << 20) |
-                      (one_pass_sort ? 0x8000000u : 0u) | ((block >> 6) << 28) | ((cc_warps & 0x7u) << 24)) |
+                      (one_pass_sort ? 0x8000000u : 0u) | (bucket_sort_on ? 0x10000000u : 0u) | ((block >> 6) << 28) | ((cc_warps & 0x7u) << 24)) |
            ((uint64_t)nbr.stride << 32);
 }
 
@@ -924,10 +945,11 @@ void World::tune_begin()
     } else if (tr.dim == 2) {
         for (int v = 6; v <= 8; v++) tr.cand[tr.ncand++] = v;
     } else if (tr.dim == 3) {
-        /* the sort: three kernels per pass (faster for ~1M keys and more)
-         * or one (faster for small scenes) */
+        /* the sort: three kernels per digit pass, one kernel per pass, or
+         * counting by bucket (when the tile sums fit its scratch) */
         tr.cand[tr.ncand++] = 0;
         tr.cand[tr.ncand++] = 1;
+        if (bucket_sort_fits()) tr.cand[tr.ncand++] = 2;
     } else if (tr.dim == 4) {
         /* threads per CTA of the density/force grids */
         const int v[3] = {64, 128, 256};
@@ -948,7 +970,7 @@ void World::tune_begin()
                 tr.ncand = 0;
                 return;
             }
-    const int prev[6] = {current_kernel(), (int)ctas_per_sm, (int)digit_bits, one_pass_sort ? 1 : 0, (int)block,
+    const int prev[6] = {current_kernel(), (int)ctas_per_sm, (int)digit_bits, sort_variant(), (int)block,
                          (int)cc_warps};
     tr.prev = prev[tr.dim];
     tr.idx = 0;
@@ -960,7 +982,7 @@ void World::tune_apply(int dim, int v)
     if (dim == 0) set_kernel(v);
     else if (dim == 1) ctas_per_sm = (uint32_t)v;
     else if (dim == 2) digit_bits = (uint32_t)v;
-    else if (dim == 3) one_pass_sort = v != 0;
+    else if (dim == 3) set_sort_variant(v);
     else if (dim == 4) block = (uint32_t)v;
     else cc_warps = (uint32_t)v;
 }
@@ -1120,10 +1142,9 @@ int World::run_stage(int stage, int flags)
         if (use_order && !needs_runs() && (!order_valid || (order_period && step_count % order_period == 0)))
             enqueue_order_refresh();
         launch_hash(L, pos, keys_u, nullptr);
-        if (!(one_pass_sort && onesweep_sort(keys_u, keys, ids, n, key_bits, digit_bits, rs, os_scratch, status_d,
-                                             stream)))
-            radix_sort(keys_u, nullptr, keys, ids, n, key_bits, digit_bits, rs, stream);
-        cudaMemsetAsync(start, 0xff, 4 * (size_t)total_buckets, stream);
+        counted_ranges = false;
+        enqueue_sort();
+        if (!counted_ranges) cudaMemsetAsync(start, 0xff, 4 * (size_t)total_buckets, stream);
         if (needs_runs()) {
             cudaMemsetAsync(nruns, 0, 4, stream);
             launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv, runs, nruns);
@@ -1254,10 +1275,7 @@ uint32_t World::launches_per_step()
     /* count by enqueueing into a capture-free dry description */
     uint32_t c = 0;
     if (stages & FG_STAGE_HASH) c += 1;
-    if (stages & FG_STAGE_SORT) {
-        const uint32_t P = radix_passes(key_bits, digit_bits);
-        c += (one_pass_sort && n && P <= 6) ? 2 + P : 3 * P;
-    }
+    if (stages & FG_STAGE_SORT) c += sort_launches();
     if (stages & FG_STAGE_RANGES) c += 1; /* + one memset node */
     if (stages & FG_STAGE_DENSITY) c += 1;
     if (nbodies) {
@@ -1781,7 +1799,11 @@ int fg_world_set_option(fg_world *w, int option, int value)
         if (value < 1 || value > 64) return FG_E_INVALID;
         W->graph_steps = (uint32_t)value;
         return FG_OK;
-    case FG_OPT_ONE_PASS_SORT: W->one_pass_sort = value != 0; return FG_OK;
+    case FG_OPT_ONE_PASS_SORT:
+        if (value < 0 || value > 2) return FG_E_INVALID;
+        W->set_sort_variant(value);
+        W->sort_chosen = true;
+        return FG_OK;
     case FG_OPT_BLOCK_SIZE:
         if (value != 64 && value != 128 && value != 256) return FG_E_INVALID;
         W->block = (uint32_t)value;
@@ -1859,7 +1881,7 @@ int fg_world_get_option(const fg_world *w, int option, int *value)
     case FG_OPT_LIST_CAP: *value = (int)W->list_cap; return FG_OK;
     case FG_OPT_LIST_AUTOGROW: *value = W->list_autogrow ? 1 : 0; return FG_OK;
     case FG_OPT_GRAPH_STEPS: *value = (int)W->graph_steps; return FG_OK;
-    case FG_OPT_ONE_PASS_SORT: *value = W->one_pass_sort ? 1 : 0; return FG_OK;
+    case FG_OPT_ONE_PASS_SORT: *value = W->sort_variant(); return FG_OK;
     case FG_OPT_CTAS_PER_SM: *value = (int)W->ctas_per_sm; return FG_OK;
     case FG_OPT_AUTOTUNE_TILES: *value = (int)W->tune_tiles; return FG_OK;
     default: return FG_E_INVALID;

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <algorithm>
 #include <vector>
 #include "fg_types.h"
 #include "fg_kernels.h"
@@ -32,6 +33,10 @@ struct Capacity {
     bool too_large() const;
 };
 
+/* worlds with at most this many buckets per particle count their keys
+ * (sort variant 2) by default */
+#define FG_BUCKET_SORT_RATIO 64
+
 struct World {
     /* layout */
     uint32_t nscenes = 0, n = 0, total_buckets = 0, nspheres = 0, nbodies = 0, total_rb_buckets = 0;
@@ -50,6 +55,30 @@ struct World {
     RadixScratch rs{nullptr, nullptr, nullptr};
     uint32_t *os_scratch = nullptr; /* one-pass sort: tile status words, digit bases, tile counters */
     bool one_pass_sort = false; /* measured slower on the 1M dam break (0.088 vs 0.076 ms) */
+    /* counting sort by bucket (sort variant 2); set_layout turns it on when
+     * the world has at most FG_BUCKET_SORT_RATIO buckets per particle */
+    bool bucket_sort_on = false;
+    bool sort_chosen = false; /* the variant was set explicitly: set_layout keeps it */
+    bool counted_ranges = false; /* this step's sort wrote start/end */
+    int sort_variant() const { return bucket_sort_on ? 2 : (one_pass_sort ? 1 : 0); }
+    void set_sort_variant(int v)
+    {
+        one_pass_sort = (v == 1);
+        bucket_sort_on = (v == 2);
+    }
+    void enqueue_sort();
+    /* the counting sort's tile sums fit the radix scratch */
+    bool bucket_sort_fits() const
+    {
+        const uint64_t tiles = ((uint64_t)total_buckets + FG_RS_TILE - 1) / FG_RS_TILE;
+        return total_buckets && tiles <= radix_hist_words((uint32_t)std::max<uint64_t>(cap.particles, 1));
+    }
+    uint32_t sort_launches() const
+    {
+        if (bucket_sort_on && bucket_sort_fits()) return n ? 5u : 2u;
+        const uint32_t P = (uint32_t)radix_passes(key_bits, digit_bits);
+        return (one_pass_sort && n && P <= 6) ? 2 + P : 3 * P;
+    }
     NbrList nbr{nullptr, nullptr, nullptr, 0, nullptr, nullptr}; /* density -> forces neighbour lists */
     uint32_t list_cap_alloc = 0; /* list slots per particle allocated (the stride) */
     uint32_t list_cap = 0;       /* entries a particle may store (<= list_cap_alloc) */

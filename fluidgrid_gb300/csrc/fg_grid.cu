@@ -358,6 +358,160 @@ cudaError_t radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_
     return e;
 }
 
+/* ------------------------------------------- counting sort by bucket
+ * Sort variant 2.  The keys are bucket indices below B (the world's total
+ * buckets), so the sort counts instead of ranking digits:
+ *   end[] zeroed, then k_bs_count adds every particle to end[key] (L2
+ *           atomics, one per run of equal keys in a warp) and keeps the
+ *           count it found there as the particle's offset in its bucket;
+ *   k_bs_tile_sums: the sum of each tile of BS_TILE counts;
+ *   k_bs_offsets: per tile, the preceding tiles' sums plus the exclusive
+ *           prefix inside the tile give P; start[k] = P[k] for an occupied
+ *           bucket, FG_EMPTY for an empty one; end[k] = P[k] + count;
+ *   k_bs_scatter: slot = start[key] + offset: keys_out[slot] = key,
+ *           tmp[slot] = particle index (in arrival order inside a bucket);
+ *   k_bs_rank: the stable order inside each bucket: particle e's rank is
+ *           the number of smaller particle indices in its bucket (a bucket
+ *           of L particles costs L loads per particle, as the density walk
+ *           over that bucket does), vals_out[start + rank] = e.
+ * The result is the stable sort: (key, particle index) ascending, and the
+ * cell ranges come with it. */
+#define BS_THREADS 256
+#define BS_ITEMS 8
+#define BS_TILE (BS_THREADS * BS_ITEMS)
+static_assert(BS_THREADS == RS_THREADS, "the tile scans use rs_block_excl");
+
+__global__ void __launch_bounds__(256) k_bs_count(const uint32_t *__restrict__ keys, uint32_t n,
+                                                 uint32_t *__restrict__ cnt, uint32_t *__restrict__ off)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    /* warp-uniform loop: a warp's 32 indices are consecutive */
+    for (uint32_t b0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b0 < n; b0 += stride) {
+        const uint32_t i = b0 + lane;
+        const bool valid = i < n;
+        const uint32_t act = __ballot_sync(0xffffffffu, valid);
+        if (valid) {
+            const uint32_t k = __ldg(keys + i);
+            const uint32_t peers = __match_any_sync(act, k);
+            const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+            uint32_t o = 0;
+            if (lane == leader) o = atomicAdd(cnt + k, (uint32_t)__popc(peers));
+            off[i] = __shfl_sync(peers, o, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+        }
+    }
+}
+
+/* one CTA per tile: the sum of its BS_TILE counts (coalesced reads) */
+__global__ void __launch_bounds__(BS_THREADS) k_bs_tile_sums(const uint32_t *__restrict__ cnt, uint32_t nb,
+                                                            uint32_t *__restrict__ tsum)
+{
+    __shared__ uint32_t s_warp[RS_WARPS + 1];
+    const size_t base = (size_t)blockIdx.x * BS_TILE;
+    uint32_t v = 0;
+#pragma unroll
+    for (int k = 0; k < BS_ITEMS; k++) {
+        const size_t i = base + (size_t)k * BS_THREADS + threadIdx.x;
+        if (i < nb) v += __ldg(cnt + i);
+    }
+    uint32_t tot;
+    rs_block_excl(v, s_warp, tot);
+    if (threadIdx.x == 0) tsum[blockIdx.x] = tot;
+}
+
+/* one CTA per tile: the tile's base (the preceding tiles' sums), then the
+ * exclusive prefix of its counts in order, staged through shared memory so
+ * that every global read and write is coalesced */
+__global__ void __launch_bounds__(BS_THREADS) k_bs_offsets(uint32_t *__restrict__ cnt_end, uint32_t nb,
+                                                          const uint32_t *__restrict__ tsum,
+                                                          uint32_t *__restrict__ start)
+{
+    __shared__ uint32_t s_c[BS_TILE];
+    __shared__ uint32_t s_warp[RS_WARPS + 1];
+    const size_t base = (size_t)blockIdx.x * BS_TILE;
+    /* the tile's base: the sum of all earlier tiles */
+    uint32_t pre = 0;
+    for (uint32_t t = threadIdx.x; t < blockIdx.x; t += BS_THREADS) pre += __ldg(tsum + t);
+    uint32_t tbase;
+    rs_block_excl(pre, s_warp, tbase);
+#pragma unroll
+    for (int k = 0; k < BS_ITEMS; k++) {
+        const size_t i = base + (size_t)k * BS_THREADS + threadIdx.x;
+        s_c[k * BS_THREADS + threadIdx.x] = i < nb ? cnt_end[i] : 0u;
+    }
+    __syncthreads();
+    /* thread t scans items t*BS_ITEMS .. +BS_ITEMS of the tile */
+    uint32_t c[BS_ITEMS], v = 0;
+#pragma unroll
+    for (int k = 0; k < BS_ITEMS; k++) {
+        c[k] = s_c[threadIdx.x * BS_ITEMS + k];
+        v += c[k];
+    }
+    uint32_t tot;
+    uint32_t p = rs_block_excl(v, s_warp, tot) + tbase;
+#pragma unroll
+    for (int k = 0; k < BS_ITEMS; k++) {
+        s_c[threadIdx.x * BS_ITEMS + k] = p; /* the bucket's first index */
+        p += c[k];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < BS_ITEMS; k++) {
+        const size_t i = base + (size_t)k * BS_THREADS + threadIdx.x;
+        if (i < nb) {
+            const uint32_t first = s_c[k * BS_THREADS + threadIdx.x];
+            const uint32_t count = cnt_end[i];
+            start[i] = count ? first : FG_EMPTY;
+            cnt_end[i] = first + count;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_bs_scatter(const uint32_t *__restrict__ keys,
+                                                   const uint32_t *__restrict__ off, uint32_t n,
+                                                   const uint32_t *__restrict__ start,
+                                                   uint32_t *__restrict__ keys_out, uint32_t *__restrict__ tmp)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = __ldg(keys + i);
+        const uint32_t slot = __ldg(start + k) + __ldg(off + i);
+        keys_out[slot] = k;
+        tmp[slot] = i;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_bs_rank(const uint32_t *__restrict__ keys_out,
+                                                const uint32_t *__restrict__ tmp, uint32_t n,
+                                                const uint32_t *__restrict__ start, const uint32_t *__restrict__ end,
+                                                uint32_t *__restrict__ vals_out)
+{
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const uint32_t k = __ldg(keys_out + s);
+        const uint32_t st = __ldg(start + k), en = __ldg(end + k);
+        const uint32_t e = __ldg(tmp + s);
+        uint32_t r = 0;
+        for (uint32_t f = st; f < en; f++) r += __ldg(tmp + f) < e ? 1u : 0u;
+        vals_out[st + r] = e;
+    }
+}
+
+bool bucket_sort(const uint32_t *keys_in, uint32_t *keys_out, uint32_t *vals_out, uint32_t n, uint32_t nbuckets,
+                 uint32_t *start, uint32_t *end, const RadixScratch &s, uint32_t scratch_words, cudaStream_t st)
+{
+    const uint32_t T = (nbuckets + BS_TILE - 1) / BS_TILE;
+    if (!nbuckets || (size_t)T > scratch_words) return false; /* the tile sums would not fit */
+    const uint32_t g = grid_for((n + 255) / 256, 8);
+    cudaMemsetAsync(end, 0, sizeof(uint32_t) * (size_t)nbuckets, st);
+    if (n) k_bs_count<<<g, 256, 0, st>>>(keys_in, n, end, s.keys_alt);
+    k_bs_tile_sums<<<T, BS_THREADS, 0, st>>>(end, nbuckets, s.hist);
+    k_bs_offsets<<<T, BS_THREADS, 0, st>>>(end, nbuckets, s.hist, start);
+    if (n) {
+        k_bs_scatter<<<g, 256, 0, st>>>(keys_in, s.keys_alt, n, start, keys_out, s.vals_alt);
+        k_bs_rank<<<g, 256, 0, st>>>(keys_out, s.vals_alt, n, start, end, vals_out);
+    }
+    return true;
+}
+
 /* ---------------------------------------------------------- onesweep
  * Stable LSD radix sort with one kernel per digit pass, after one histogram
  * kernel for all passes (decoupled look-back):

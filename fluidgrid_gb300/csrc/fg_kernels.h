@@ -57,6 +57,15 @@ bool onesweep_sort(const uint32_t *keys_in, uint32_t *keys_out, uint32_t *vals_o
 cudaError_t radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
                 uint32_t n, uint32_t bits, uint32_t digit_bits, const RadixScratch &s, cudaStream_t st);
 
+/* Counting sort by bucket (keys below nbuckets): the same result as
+ * radix_sort with vals_in = 0..n-1, and it writes start[] (0xffffffff for
+ * empty buckets) and end[] of every occupied bucket of [0, nbuckets) on the
+ * way.  Uses s.keys_alt and s.vals_alt (n words each) and s.hist
+ * (scratch_words words; returns false, doing nothing, when the
+ * ceil(nbuckets / 2048) tile sums exceed them). */
+bool bucket_sort(const uint32_t *keys_in, uint32_t *keys_out, uint32_t *vals_out, uint32_t n, uint32_t nbuckets,
+                 uint32_t *start, uint32_t *end, const RadixScratch &s, uint32_t scratch_words, cudaStream_t st);
+
 /* start[] must be pre-filled with 0xffffffff over the bucket range.
  * inv (optional) receives particle -> sorted index; runs (optional) receives
  * the first sorted index of every occupied bucket, in no particular order,

@@ -223,10 +223,14 @@ int fg_world_set_graphs(fg_world *w, int on);
  *                         stay those of FG_OPT_CTAS_PER_SM
  *   FG_OPT_RUNS_PER_CTA   kernel 2: bucket runs in flight per CTA (one warp
  *                         each), 1, 2 or 4 (default)
- *   FG_OPT_ONE_PASS_SORT  1 = the fluid sort runs one kernel per digit pass
- *                         (decoupled look-back); 0 = upsweep, scan and
- *                         downsweep kernels per pass (default).  Same order
- *                         either way.
+ *   FG_OPT_ONE_PASS_SORT  the fluid sort's variant: 0 = upsweep, scan and
+ *                         downsweep kernels per digit pass; 1 = one kernel
+ *                         per pass (decoupled look-back); 2 = counting by
+ *                         bucket (a histogram of the keys, a scan that
+ *                         writes the cell ranges, a scatter, a stable rank
+ *                         inside each bucket).  Default: 2 for worlds with at
+ *                         most 64 buckets per particle, else 0.  The same
+ *                         order and cell ranges from each.
  * Kernels 0 and 1 (with either target order) produce bit-identical states;
  * kernel 2 sums the same terms in another order.  No kernel's results depend
  * on CTAs per SM or digit width, and kernel 1's not on the list capacity

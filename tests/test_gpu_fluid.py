@@ -225,7 +225,7 @@ def test_autotuner_keeps_results_and_reports():
         res.append((p, v))
         w.close()
     assert st["steps_per_kernel"][1] == 12
-    assert w_ctas in (16, 32, 64) and 6 <= st["digit_bits"] <= 8 and st["one_pass_sort"] in (0, 1)
+    assert w_ctas in (16, 32, 64) and 6 <= st["digit_bits"] <= 8 and st["one_pass_sort"] in (0, 1, 2)
     assert st["block_size"] in (64, 128, 256)
     for a, b in zip(res[0], res[1]):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
@@ -478,29 +478,54 @@ def test_empty_scene_in_world():
     w.close()
 
 
-@pytest.mark.parametrize("name", ["dam_break_16k", "odd_buckets", "ragged_4097", "ragged_1"])
-def test_one_pass_sort_equals_three_kernel_sort(name):
-    """The one-kernel-per-pass sort (decoupled look-back) and the upsweep /
-    scan / downsweep passes produce the same sorted keys, order and cell
-    ranges, so the evolved state is bit-identical."""
-    spec = VARIANTS[name]
+@pytest.mark.parametrize("name", ["dam_break_16k", "odd_buckets", "ragged_4097", "ragged_1", "ragged_7",
+                                  "far_origin", "one_bucket"])
+def test_sort_variants_equal(name):
+    """The three sort variants produce the same sorted keys, order and cell
+    ranges, so the evolved state is bit-identical: the upsweep / scan /
+    downsweep radix passes (0), one kernel per pass with decoupled look-back
+    (1) and the counting sort by bucket (2), which writes start/end itself.
+    `one_bucket` puts 4,097 particles in a single bucket (one run)."""
+    if name == "one_bucket":
+        p = np.ones((4097, 4), np.float32)
+        p[:, :3] = np.random.default_rng(9).uniform(0.1, 0.3, (4097, 3))
+        spec = SceneSpec(pos=p, buckets=(1, 1, 1), name="one_bucket")
+    else:
+        spec = VARIANTS[name]
     outs = []
-    for one in (1, 0):
+    for variant in (0, 1, 2):
         w = World([spec])
         w.set_option("autotune_period", 0)
-        w.set_option("one_pass_sort", one)
-        assert w.get_option("one_pass_sort") == one
+        w.set_option("one_pass_sort", variant)
+        assert w.get_option("one_pass_sort") == variant
         w.step(3)
-        outs.append([w.read(k) for k in ("KEYS", "IDS", "START", "SPOS")] + list(w.download()))
+        st, en = w.read("START"), w.read("END")
+        occ = st != 0xFFFFFFFF
+        outs.append([w.read(k) for k in ("KEYS", "IDS", "SPOS")] + [st, en[occ]] + list(w.download()))
         w.close()
-    for a, b in zip(*outs):
-        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
-def test_one_pass_sort_large_against_numpy():
-    """3M particles in 2^21 buckets: 1,465 tiles, more than the GPU holds at
-    once, so tiles look back across tiles that ran earlier and left.  Keys
-    and order equal a stable numpy sort of the hash keys."""
+def test_counting_sort_is_the_default_for_dense_bucket_tables():
+    """A world with at most 64 buckets per particle counts its keys; one
+    with more sorts them by digits."""
+    w = World([VARIANTS["dam_break_16k"]])  # 2^18 buckets, 16,384 particles
+    assert w.get_option("one_pass_sort") == 2
+    w.close()
+    w = World([VARIANTS["ragged_7"]])  # 4,096 buckets, 7 particles
+    assert w.get_option("one_pass_sort") in (0, 1)
+    w.close()
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_sort_large_against_numpy(variant):
+    """3M particles in 2^21 buckets.  One pass per kernel: 1,465 tiles, more
+    than the GPU holds at once, so tiles look back across tiles that ran
+    earlier and left.  Counting: 1,024 bucket tiles, 3M atomics.  Keys and
+    order equal a stable numpy sort of the hash keys; the counting sort's
+    cell ranges equal numpy's."""
     rng = np.random.default_rng(21)
     n = 3 * 1024 * 1024
     pos = np.ones((n, 4), np.float32)
@@ -508,15 +533,24 @@ def test_one_pass_sort_large_against_numpy():
     spec = SceneSpec(pos=pos, box_min=(0, 0, 0), box_max=(4, 4, 4), buckets=(128, 128, 128), name="cloud_3m")
     w = World([spec])
     w.set_option("autotune_period", 0)
-    w.set_option("one_pass_sort", 1)
+    w.set_option("one_pass_sort", variant)
     w.set_stages(1 | 2)  # hash and sort only
     w.step(1)
     ku, ks, ids = w.read("KEYS_UNSORTED"), w.read("KEYS"), w.read("IDS")
+    st, en = w.read("START"), w.read("END")
     w.sync()
     w.close()
     order = np.argsort(ku, kind="stable")
     assert np.array_equal(ids, order.astype(np.uint32))
     assert np.array_equal(ks, ku[order])
+    if variant == 2:
+        nb = 128 ** 3
+        cnt = np.bincount(ku, minlength=nb)
+        first = np.concatenate([[0], np.cumsum(cnt)[:-1]])
+        occ = cnt > 0
+        assert np.array_equal(st[occ], first[occ].astype(np.uint32))
+        assert (st[~occ] == 0xFFFFFFFF).all()
+        assert np.array_equal(en[occ], (first + cnt)[occ].astype(np.uint32))
 
 
 def test_sort_lookback_wait_is_bounded():
