@@ -663,14 +663,19 @@ void World::enqueue_bodies(cudaStream_t st, float4 *vf)
 
 /* The fluid sort of the variant in use: keys_u -> keys, ids (and, for the
  * counting sort, start/end). */
-void World::enqueue_sort()
+void World::enqueue_sort(bool with_ranges)
 {
+    /* with_ranges: the step's ranges pass follows directly; the counting
+     * sort then does its reorder too (fused_ranges) */
+    BucketReorder R{pos, vel, spos, svel, inv, needs_runs() ? runs : nullptr, nruns};
+    if (bucket_sort_on && with_ranges && needs_runs()) cudaMemsetAsync(nruns, 0, 4, stream);
     if (bucket_sort_on &&
         bucket_sort(keys_u, keys, ids, n, total_buckets, start, end, rs,
                     (uint32_t)std::min<size_t>(radix_hist_words((uint32_t)std::max<uint64_t>(cap.particles, 1)),
                                                0xffffffffu),
-                    stream)) {
+                    stream, with_ranges ? &R : nullptr)) {
         counted_ranges = true;
+        fused_ranges = with_ranges;
         return;
     }
     if (one_pass_sort && onesweep_sort(keys_u, keys, ids, n, key_bits, digit_bits, rs, os_scratch, status_d, stream))
@@ -717,26 +722,29 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         mark(0, 1);
         launches++;
     }
-    counted_ranges = false;
+    counted_ranges = fused_ranges = false;
     if (stages & FG_STAGE_SORT) {
         mark(1, 0);
-        enqueue_sort();
+        /* an end-to-end step's ranges wait for the velocity upload: no fused reorder */
+        enqueue_sort((stages & FG_STAGE_RANGES) && !(cur_io && iob));
         launches += sort_launches();
         mark(1, 1);
     }
     if (cur_io && iob) CK0(cudaStreamWaitEvent(stream, ev_vel_in, 0));
     if (stages & FG_STAGE_RANGES) {
         mark(2, 0);
-        /* the counting sort wrote start[] of every bucket already */
-        if (!counted_ranges) cudaMemsetAsync(start, 0xff, 4 * (size_t)total_buckets, stream);
-        if (needs_runs()) {
-            cudaMemsetAsync(nruns, 0, 4, stream);
-            launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv, runs, nruns);
-        } else {
-            launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv);
+        if (!fused_ranges) {
+            /* the counting sort wrote start[] of every bucket already */
+            if (!counted_ranges) cudaMemsetAsync(start, 0xff, 4 * (size_t)total_buckets, stream);
+            if (needs_runs()) {
+                cudaMemsetAsync(nruns, 0, 4, stream);
+                launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv, runs, nruns);
+            } else {
+                launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv);
+            }
+            launches += 1;
         }
         mark(2, 1);
-        launches += 1;
     }
     /* with a full step forked, the body reduction and integration follow the
      * contact on the second stream and overlap the force pass, which reads
@@ -1142,14 +1150,16 @@ int World::run_stage(int stage, int flags)
         if (use_order && !needs_runs() && (!order_valid || (order_period && step_count % order_period == 0)))
             enqueue_order_refresh();
         launch_hash(L, pos, keys_u, nullptr);
-        counted_ranges = false;
-        enqueue_sort();
-        if (!counted_ranges) cudaMemsetAsync(start, 0xff, 4 * (size_t)total_buckets, stream);
-        if (needs_runs()) {
-            cudaMemsetAsync(nruns, 0, 4, stream);
-            launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv, runs, nruns);
-        } else {
-            launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv);
+        counted_ranges = fused_ranges = false;
+        enqueue_sort(true);
+        if (!fused_ranges) {
+            if (!counted_ranges) cudaMemsetAsync(start, 0xff, 4 * (size_t)total_buckets, stream);
+            if (needs_runs()) {
+                cudaMemsetAsync(nruns, 0, 4, stream);
+                launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv, runs, nruns);
+            } else {
+                launch_cell_ranges(keys, ids, pos, vel, start, end, spos, svel, n, stream, inv);
+            }
         }
         break;
     }
@@ -1276,7 +1286,8 @@ uint32_t World::launches_per_step()
     uint32_t c = 0;
     if (stages & FG_STAGE_HASH) c += 1;
     if (stages & FG_STAGE_SORT) c += sort_launches();
-    if (stages & FG_STAGE_RANGES) c += 1; /* + one memset node */
+    /* + one memset node; none with the counting sort's fused reorder */
+    if ((stages & FG_STAGE_RANGES) && !(bucket_sort_on && bucket_sort_fits() && (stages & FG_STAGE_SORT))) c += 1;
     if (stages & FG_STAGE_DENSITY) c += 1;
     if (nbodies) {
         if (stages & FG_STAGE_RB_GRID) /* aabb reset, hash, sort + ranges */

@@ -60,13 +60,14 @@ struct World {
     bool bucket_sort_on = false;
     bool sort_chosen = false; /* the variant was set explicitly: set_layout keeps it */
     bool counted_ranges = false; /* this step's sort wrote start/end */
+    bool fused_ranges = false;   /* ... and did the ranges pass's reorder */
     int sort_variant() const { return bucket_sort_on ? 2 : (one_pass_sort ? 1 : 0); }
     void set_sort_variant(int v)
     {
         one_pass_sort = (v == 1);
         bucket_sort_on = (v == 2);
     }
-    void enqueue_sort();
+    void enqueue_sort(bool with_ranges = false);
     /* the counting sort's tile sums fit the radix scratch */
     bool bucket_sort_fits() const
     {
@@ -75,7 +76,7 @@ struct World {
     }
     uint32_t sort_launches() const
     {
-        if (bucket_sort_on && bucket_sort_fits()) return n ? 5u : 2u;
+        if (bucket_sort_on && bucket_sort_fits()) return n ? 5u : 2u; /* the fused reorder included */
         const uint32_t P = (uint32_t)radix_passes(key_bits, digit_bits);
         return (one_pass_sort && n && P <= 6) ? 2 + P : 3 * P;
     }

@@ -495,8 +495,48 @@ __global__ void __launch_bounds__(256) k_bs_rank(const uint32_t *__restrict__ ke
     }
 }
 
+/* k_bs_rank and the ranges pass's reorder in one: the particle's sorted
+ * index p = start + rank gets its id, position and velocity, inv[id] = p,
+ * and a rank-0 particle appends its bucket's first index to runs (in no
+ * particular order, as the ranges pass does). */
+__global__ void __launch_bounds__(256) k_bs_rank_reorder(const uint32_t *__restrict__ keys_out,
+                                                        const uint32_t *__restrict__ tmp, uint32_t n,
+                                                        const uint32_t *__restrict__ start,
+                                                        const uint32_t *__restrict__ end,
+                                                        uint32_t *__restrict__ vals_out, BucketReorder R)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t b0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b0 < n; b0 += stride) {
+        const uint32_t s = b0 + lane;
+        const bool valid = s < n;
+        uint32_t st = 0, r = 0;
+        if (valid) {
+            const uint32_t k = __ldg(keys_out + s);
+            st = __ldg(start + k);
+            const uint32_t en = __ldg(end + k);
+            const uint32_t e = __ldg(tmp + s);
+            for (uint32_t f = st; f < en; f++) r += __ldg(tmp + f) < e ? 1u : 0u;
+            const uint32_t p = st + r;
+            vals_out[p] = e;
+            R.spos[p] = __ldg(R.pos + e);
+            if (R.vel) R.svel[p] = __ldg(R.vel + e);
+            if (R.inv) R.inv[e] = p;
+        }
+        if (R.runs) {
+            const bool head = valid && r == 0u;
+            const uint32_t m = __ballot_sync(0xffffffffu, head);
+            uint32_t base = 0;
+            if (lane == 0 && m) base = atomicAdd(R.nruns, (uint32_t)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (head) R.runs[base + __popc(m & ((1u << lane) - 1u))] = st;
+        }
+    }
+}
+
 bool bucket_sort(const uint32_t *keys_in, uint32_t *keys_out, uint32_t *vals_out, uint32_t n, uint32_t nbuckets,
-                 uint32_t *start, uint32_t *end, const RadixScratch &s, uint32_t scratch_words, cudaStream_t st)
+                 uint32_t *start, uint32_t *end, const RadixScratch &s, uint32_t scratch_words, cudaStream_t st,
+                 const BucketReorder *reorder)
 {
     const uint32_t T = (nbuckets + BS_TILE - 1) / BS_TILE;
     if (!nbuckets || (size_t)T > scratch_words) return false; /* the tile sums would not fit */
@@ -507,7 +547,10 @@ bool bucket_sort(const uint32_t *keys_in, uint32_t *keys_out, uint32_t *vals_out
     k_bs_offsets<<<T, BS_THREADS, 0, st>>>(end, nbuckets, s.hist, start);
     if (n) {
         k_bs_scatter<<<g, 256, 0, st>>>(keys_in, s.keys_alt, n, start, keys_out, s.vals_alt);
-        k_bs_rank<<<g, 256, 0, st>>>(keys_out, s.vals_alt, n, start, end, vals_out);
+        if (reorder)
+            k_bs_rank_reorder<<<g, 256, 0, st>>>(keys_out, s.vals_alt, n, start, end, vals_out, *reorder);
+        else
+            k_bs_rank<<<g, 256, 0, st>>>(keys_out, s.vals_alt, n, start, end, vals_out);
     }
     return true;
 }

@@ -63,8 +63,16 @@ cudaError_t radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_
  * way.  Uses s.keys_alt and s.vals_alt (n words each) and s.hist
  * (scratch_words words; returns false, doing nothing, when the
  * ceil(nbuckets / 2048) tile sums exceed them). */
+struct BucketReorder {
+    const float4 *pos, *vel; /* unsorted (vel may be null) */
+    float4 *spos, *svel;
+    uint32_t *inv, *runs, *nruns; /* optional; nruns zeroed by the caller */
+};
+/* With reorder, the stable rank also does launch_cell_ranges' gathers
+ * (sorted position and velocity, inv, run heads): no ranges pass needed. */
 bool bucket_sort(const uint32_t *keys_in, uint32_t *keys_out, uint32_t *vals_out, uint32_t n, uint32_t nbuckets,
-                 uint32_t *start, uint32_t *end, const RadixScratch &s, uint32_t scratch_words, cudaStream_t st);
+                 uint32_t *start, uint32_t *end, const RadixScratch &s, uint32_t scratch_words, cudaStream_t st,
+                 const BucketReorder *reorder = nullptr);
 
 /* start[] must be pre-filled with 0xffffffff over the bucket range.
  * inv (optional) receives particle -> sorted index; runs (optional) receives
