@@ -663,17 +663,40 @@ void World::enqueue_bodies(cudaStream_t st, float4 *vf)
 
 /* The fluid sort of the variant in use: keys_u -> keys, ids (and, for the
  * counting sort, start/end). */
+uint32_t World::sort_launches() const
+{
+    /* the fused reorder included; the count runs in the hash pass when the
+     * step hashes too */
+    if (bucket_sort_on && bucket_sort_fits()) return n ? ((stages & FG_STAGE_HASH) ? 4u : 5u) : 2u;
+    const uint32_t P = (uint32_t)radix_passes(key_bits, digit_bits);
+    return (one_pass_sort && n && P <= 6) ? 2 + P : 3 * P;
+}
+
+/* The hash pass; when the counting sort follows, it counts the keys too. */
+void World::enqueue_hash(const Launch &L, bool sort_follows)
+{
+    counted_in_hash = sort_follows && bucket_sort_on && bucket_sort_fits();
+    if (counted_in_hash) {
+        cudaMemsetAsync(end, 0, 4 * (size_t)total_buckets, stream);
+        launch_hash(L, pos, keys_u, nullptr, end, rs.keys_alt);
+    } else {
+        launch_hash(L, pos, keys_u, nullptr);
+    }
+}
+
 void World::enqueue_sort(bool with_ranges)
 {
     /* with_ranges: the step's ranges pass follows directly; the counting
      * sort then does its reorder too (fused_ranges) */
     BucketReorder R{pos, vel, spos, svel, inv, needs_runs() ? runs : nullptr, nruns};
     if (bucket_sort_on && with_ranges && needs_runs()) cudaMemsetAsync(nruns, 0, 4, stream);
+    const bool counted = counted_in_hash;
+    counted_in_hash = false;
     if (bucket_sort_on &&
         bucket_sort(keys_u, keys, ids, n, total_buckets, start, end, rs,
                     (uint32_t)std::min<size_t>(radix_hist_words((uint32_t)std::max<uint64_t>(cap.particles, 1)),
                                                0xffffffffu),
-                    stream, with_ranges ? &R : nullptr)) {
+                    stream, with_ranges ? &R : nullptr, counted)) {
         counted_ranges = true;
         fused_ranges = with_ranges;
         return;
@@ -716,9 +739,10 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         CK0(cudaEventRecord(ev_vel_in, stream3));
         CK0(cudaMemcpyAsync(pos, cur_io->hp, iob, cudaMemcpyHostToDevice, stream));
     }
+    counted_in_hash = false;
     if (stages & FG_STAGE_HASH) {
         mark(0, 0);
-        launch_hash(L, pos, keys_u, nullptr);
+        enqueue_hash(L, (stages & FG_STAGE_SORT) != 0);
         mark(0, 1);
         launches++;
     }
@@ -1149,7 +1173,7 @@ int World::run_stage(int stage, int flags)
         }
         if (use_order && !needs_runs() && (!order_valid || (order_period && step_count % order_period == 0)))
             enqueue_order_refresh();
-        launch_hash(L, pos, keys_u, nullptr);
+        enqueue_hash(L, true);
         counted_ranges = fused_ranges = false;
         enqueue_sort(true);
         if (!fused_ranges) {

@@ -68,18 +68,15 @@ struct World {
         bucket_sort_on = (v == 2);
     }
     void enqueue_sort(bool with_ranges = false);
+    void enqueue_hash(const Launch &L, bool sort_follows);
+    bool counted_in_hash = false; /* this step's hash pass counted the keys for the counting sort */
     /* the counting sort's tile sums fit the radix scratch */
     bool bucket_sort_fits() const
     {
         const uint64_t tiles = ((uint64_t)total_buckets + FG_RS_TILE - 1) / FG_RS_TILE;
         return total_buckets && tiles <= radix_hist_words((uint32_t)std::max<uint64_t>(cap.particles, 1));
     }
-    uint32_t sort_launches() const
-    {
-        if (bucket_sort_on && bucket_sort_fits()) return n ? 5u : 2u; /* the fused reorder included */
-        const uint32_t P = (uint32_t)radix_passes(key_bits, digit_bits);
-        return (one_pass_sort && n && P <= 6) ? 2 + P : 3 * P;
-    }
+    uint32_t sort_launches() const;
     NbrList nbr{nullptr, nullptr, nullptr, 0, nullptr, nullptr}; /* density -> forces neighbour lists */
     uint32_t list_cap_alloc = 0; /* list slots per particle allocated (the stride) */
     uint32_t list_cap = 0;       /* entries a particle may store (<= list_cap_alloc) */

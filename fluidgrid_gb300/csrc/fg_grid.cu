@@ -36,30 +36,47 @@ uint32_t grid_for(uint32_t nwork, int ctas_per_sm)
 /* ------------------------------------------------------------- hashing */
 
 /* CalcHashKeyK (K_HashGrid.cu:26-38): key = bucket_base + HashKeyD(pos),
- * id = particle index. */
+ * id = particle index.  With cnt, also the counting sort's first pass (as
+ * k_bs_count): cnt[key] += 1 by L2 atomics, one per run of equal keys in a
+ * warp, and off[i] = the count found there. */
 __global__ void __launch_bounds__(FG_CHUNK) k_hash(const FgWork *__restrict__ work, uint32_t nwork, uint32_t n_single,
                                                   const FgScene *__restrict__ table,
                                                   const __grid_constant__ FgScene single,
                                                   const float4 *__restrict__ pos, uint32_t *__restrict__ keys,
-                                                  uint32_t *__restrict__ ids)
+                                                  uint32_t *__restrict__ ids, uint32_t *__restrict__ cnt,
+                                                  uint32_t *__restrict__ off)
 {
+    const uint32_t lane = threadIdx.x & 31u;
     for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
         FgWork it = fg_work(work, w, n_single);
         const FgScene *S = fg_scene(table, &single, it.scene);
-        if (threadIdx.x < it.count) {
-            uint32_t i = it.first + threadIdx.x;
+        const bool valid = threadIdx.x < it.count;
+        const uint32_t i = it.first + threadIdx.x;
+        uint32_t k = 0;
+        if (valid) {
             float4 p = __ldg(pos + i);
-            keys[i] = S->bucket_base + fg_hash(p.x, p.y, p.z, S->cell, S->nb, S->nb_mask);
+            k = S->bucket_base + fg_hash(p.x, p.y, p.z, S->cell, S->nb, S->nb_mask);
+            keys[i] = k;
             if (ids) ids[i] = i;
+        }
+        if (cnt) { /* uniform: every lane of the warp gets here */
+            const uint32_t act = __ballot_sync(0xffffffffu, valid);
+            if (valid) {
+                const uint32_t peers = __match_any_sync(act, k);
+                const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+                uint32_t o = 0;
+                if (lane == leader) o = atomicAdd(cnt + k, (uint32_t)__popc(peers));
+                off[i] = __shfl_sync(peers, o, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+            }
         }
     }
 }
 
-void launch_hash(const Launch &L, const float4 *pos, uint32_t *keys, uint32_t *ids)
+void launch_hash(const Launch &L, const float4 *pos, uint32_t *keys, uint32_t *ids, uint32_t *cnt, uint32_t *off)
 {
     if (!L.nwork) return;
     k_hash<<<grid_for(L.nwork, 64), FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, pos, keys,
-                                                             ids);
+                                                             ids, cnt, off);
 }
 
 /* CalcHashKeyWithOffsetK (K_HashGrid.cu:43-63): world = conj(q)*p*q + cm of
@@ -536,13 +553,15 @@ __global__ void __launch_bounds__(256) k_bs_rank_reorder(const uint32_t *__restr
 
 bool bucket_sort(const uint32_t *keys_in, uint32_t *keys_out, uint32_t *vals_out, uint32_t n, uint32_t nbuckets,
                  uint32_t *start, uint32_t *end, const RadixScratch &s, uint32_t scratch_words, cudaStream_t st,
-                 const BucketReorder *reorder)
+                 const BucketReorder *reorder, bool counted)
 {
     const uint32_t T = (nbuckets + BS_TILE - 1) / BS_TILE;
     if (!nbuckets || (size_t)T > scratch_words) return false; /* the tile sums would not fit */
     const uint32_t g = grid_for((n + 255) / 256, 8);
-    cudaMemsetAsync(end, 0, sizeof(uint32_t) * (size_t)nbuckets, st);
-    if (n) k_bs_count<<<g, 256, 0, st>>>(keys_in, n, end, s.keys_alt);
+    if (!counted) {
+        cudaMemsetAsync(end, 0, sizeof(uint32_t) * (size_t)nbuckets, st);
+        if (n) k_bs_count<<<g, 256, 0, st>>>(keys_in, n, end, s.keys_alt);
+    }
     k_bs_tile_sums<<<T, BS_THREADS, 0, st>>>(end, nbuckets, s.hist);
     k_bs_offsets<<<T, BS_THREADS, 0, st>>>(end, nbuckets, s.hist, start);
     if (n) {

@@ -26,7 +26,10 @@ int sm_count();
 uint32_t grid_for(uint32_t nwork, int ctas_per_sm);
 
 /* ---- grid build (fg_grid.cu) ---- */
-void launch_hash(const Launch &L, const float4 *pos, uint32_t *keys, uint32_t *ids);
+/* cnt/off (optional): the counting sort's first pass fused in (cnt zeroed
+ * over the world's buckets by the caller; off = its s.keys_alt) */
+void launch_hash(const Launch &L, const float4 *pos, uint32_t *keys, uint32_t *ids, uint32_t *cnt = nullptr,
+                 uint32_t *off = nullptr);
 void launch_hash_with_offset(const Launch &L, const float4 *local, const float4 *cm, const float4 *q,
                              float4 *world, uint32_t *keys, uint32_t *ids, int *aabb /* 6 ints per scene or null */);
 
@@ -69,10 +72,12 @@ struct BucketReorder {
     uint32_t *inv, *runs, *nruns; /* optional; nruns zeroed by the caller */
 };
 /* With reorder, the stable rank also does launch_cell_ranges' gathers
- * (sorted position and velocity, inv, run heads): no ranges pass needed. */
+ * (sorted position and velocity, inv, run heads): no ranges pass needed.
+ * counted: launch_hash already counted the keys into end[] and left the
+ * arrival offsets in s.keys_alt. */
 bool bucket_sort(const uint32_t *keys_in, uint32_t *keys_out, uint32_t *vals_out, uint32_t n, uint32_t nbuckets,
                  uint32_t *start, uint32_t *end, const RadixScratch &s, uint32_t scratch_words, cudaStream_t st,
-                 const BucketReorder *reorder = nullptr);
+                 const BucketReorder *reorder = nullptr, bool counted = false);
 
 /* start[] must be pre-filled with 0xffffffff over the bucket range.
  * inv (optional) receives particle -> sorted index; runs (optional) receives
