@@ -423,7 +423,8 @@ def run_served(duration=60.0, rate=200.0, budget=120 << 30, seed=0x5EED, pipelin
     cfg = _ffi.fg_server_config()
     _ffi.load().fg_server_config_defaults(ctypes.byref(cfg))
     policy = {"hbm_budget_bytes": budget, "max_particles_per_step": int(cfg.max_particles),
-              "target_step_ms": round(float(cfg.target_step_ms), 3), "head_wait_s": round(float(cfg.head_wait_s), 3)}
+              "target_step_ms": round(float(cfg.target_step_ms), 3), "head_wait_s": round(float(cfg.head_wait_s), 3),
+              "autotune_period": int(cfg.autotune_period)}
     srv = Server(budget_bytes=budget, pipeline_depth=pipeline_depth)
     ids = []
     infos = []

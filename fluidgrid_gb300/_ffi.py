@@ -67,7 +67,7 @@ class fg_scene_desc(ctypes.Structure):
 class fg_server_config(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_particles", c_u32), ("max_admit_per_step", c_u32),
                 ("use_graphs", ctypes.c_int), ("grow_via_host", ctypes.c_int), ("pipeline_depth", ctypes.c_int),
-                ("target_step_ms", c_f), ("head_wait_s", c_f), ("reserved", ctypes.c_int)]
+                ("target_step_ms", c_f), ("head_wait_s", c_f), ("autotune_period", ctypes.c_int)]
 
 
 class fg_server_step_info(ctypes.Structure):

@@ -210,13 +210,14 @@ int Server::relayout()
         /* the budget charges list memory at the admission-time capacity: the
          * lists do not grow (denser particles walk their buckets instead) */
         nw->list_autogrow = false;
+        /* trials of slower launch shapes would land in the step latency */
+        nw->tune_period = (uint32_t)std::max(cfg.autotune_period, 0);
         if (w) {
             nw->list_cap_alloc = w->list_cap_alloc;
             nw->digit_bits = w->digit_bits;
             nw->ctas_per_sm = w->ctas_per_sm;
             nw->block = w->block;
             nw->cc_warps = w->cc_warps;
-            nw->tune_period = w->tune_period;
             nw->use_graphs = w->use_graphs;
             size_t free_b = 0, total_b = 0;
             CK(cudaMemGetInfo(&free_b, &total_b));

@@ -356,7 +356,10 @@ typedef struct fg_server_config {
                                      not fit, it gets a reservation: a younger request is admitted
                                      only if it fits now and finishes before enough resident scenes
                                      have left for the oldest to fit (backfilling); default 0 */
-    int reserved;
+    int autotune_period;          /* steps between autotuning rounds of the resident world; 0 = no
+                                     autotuning (default: a round's trial steps of other launch
+                                     shapes land in the step latency; measured on the C5 arrivals,
+                                     off gave 3% more throughput and a lower p99) */
 } fg_server_config;
 enum { FG_REQ_QUEUED = 0, FG_REQ_ACTIVE = 1, FG_REQ_DONE = 2 };
 typedef struct fg_server_step_info {
