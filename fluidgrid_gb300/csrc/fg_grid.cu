@@ -378,9 +378,10 @@ cudaError_t radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_
 /* ------------------------------------------- counting sort by bucket
  * Sort variant 2.  The keys are bucket indices below B (the world's total
  * buckets), so the sort counts instead of ranking digits:
- *   end[] zeroed, then k_bs_count adds every particle to end[key] (L2
- *           atomics, one per run of equal keys in a warp) and keeps the
- *           count it found there as the particle's offset in its bucket;
+ *   end[] zeroed, then k_bs_count (or k_hash, when the step hashes right
+ *           before) adds every particle to end[key] (L2 atomics, one per run
+ *           of equal keys in a warp) and keeps the count it found there as
+ *           the particle's offset in its bucket;
  *   k_bs_tile_sums: the sum of each tile of BS_TILE counts;
  *   k_bs_offsets: per tile, the preceding tiles' sums plus the exclusive
  *           prefix inside the tile give P; start[k] = P[k] for an occupied
@@ -390,7 +391,8 @@ cudaError_t radix_sort(const uint32_t *keys_in, const uint32_t *vals_in, uint32_
  *   k_bs_rank: the stable order inside each bucket: particle e's rank is
  *           the number of smaller particle indices in its bucket (a bucket
  *           of L particles costs L loads per particle, as the density walk
- *           over that bucket does), vals_out[start + rank] = e.
+ *           over that bucket does), vals_out[start + rank] = e;
+ *           k_bs_rank_reorder also does the ranges pass's gathers there.
  * The result is the stable sort: (key, particle index) ascending, and the
  * cell ranges come with it. */
 #define BS_THREADS 256
