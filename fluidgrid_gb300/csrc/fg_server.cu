@@ -63,6 +63,13 @@ struct Request {
 #define FG_SERVER_RING 16 /* pipeline_depth is clamped below this */
 #define FG_STEP_FIXED_MS 0.1 /* predicted per-step time independent of the particle count */
 #define FG_RATE_MIN_N 100000u /* steps of fewer particles do not update the learned rate */
+/* neighbour-list slots per particle of a server world: they do not grow
+ * (the budget charges them at admission), so they cover the compressed
+ * phase's ~300 in-range visits; a particle with more walks its buckets in
+ * the force pass */
+#ifndef FG_SERVER_LIST_CAP
+#define FG_SERVER_LIST_CAP 320u
+#endif
 
 struct Server {
     fg_server_config cfg;
@@ -201,7 +208,7 @@ int Server::relayout()
             c.work = g(need.work, w->cap.work);
             c.work_sph = g(need.work_sph, w->cap.work_sph);
         }
-        const uint32_t lc = w ? w->list_cap_alloc : FG_LIST_CAP_DEFAULT;
+        const uint32_t lc = w ? w->list_cap_alloc : FG_SERVER_LIST_CAP;
         /* headroom only while the world stays within the budget */
         if (c.too_large() || World::footprint(c, lc) > cfg.hbm_budget_bytes) c = need;
         nw.reset(new World());
@@ -210,6 +217,7 @@ int Server::relayout()
         /* the budget charges list memory at the admission-time capacity: the
          * lists do not grow (denser particles walk their buckets instead) */
         nw->list_autogrow = false;
+        nw->list_cap_alloc = lc;
         /* trials of slower launch shapes would land in the step latency */
         nw->tune_period = (uint32_t)std::max(cfg.autotune_period, 0);
         if (w) {
@@ -330,7 +338,7 @@ int Server::step(fg_server_step_info *info)
     const double tw0 = now();
     uint32_t admitted = 0;
     /* admission: arrival order, a request that does not fit yet is skipped */
-    const uint32_t lc = w ? w->list_cap_alloc : FG_LIST_CAP_DEFAULT;
+    const uint32_t lc = w ? w->list_cap_alloc : FG_SERVER_LIST_CAP;
     const double tnow = now();
     /* particles one step may advance: the particle limit and what the time
      * budget allows at the learned rate */
@@ -428,8 +436,8 @@ void fg_server_config_defaults(fg_server_config *c)
      * per step; with backfilling this kept the C5 arrival workload's p99
      * step latency under 1.9 ms for every scene size (admitting by the HBM
      * budget alone: p99 210 ms) */
-    c->max_particles = 850000u;
-    c->target_step_ms = 0.9f;
+    c->max_particles = 1200000u;
+    c->target_step_ms = 1.1f;
     c->head_wait_s = 0.0f;
 }
 
@@ -479,7 +487,7 @@ int fg_server_submit(fg_server *srv, const fg_scene_desc *d, uint32_t steps, uin
         q->bodies[b].local_spheres = q->spheres[b].data();
     }
     q->desc.bodies = d->n_bodies ? q->bodies.data() : nullptr;
-    const uint32_t lc = S->w ? S->w->list_cap_alloc : FG_LIST_CAP_DEFAULT;
+    const uint32_t lc = S->w ? S->w->list_cap_alloc : FG_SERVER_LIST_CAP;
     if (scene_bytes(q->desc, lc) > S->cfg.hbm_budget_bytes ||
         (S->cfg.max_particles && d->n_particles > S->cfg.max_particles)) {
         set_error_msg("scene alone exceeds the server budget");

@@ -338,7 +338,7 @@ int fg_selftest_bounded_wait(unsigned int spin_limit, unsigned int *flags);
 typedef struct fg_server fg_server;
 typedef struct fg_server_config {
     size_t hbm_budget_bytes;      /* device bytes the resident scenes may use */
-    uint32_t max_particles;       /* particles advanced per step, 0 = no limit (default 850,000;
+    uint32_t max_particles;       /* particles advanced per step, 0 = no limit (default 1,200,000;
                                      a larger scene is refused with FG_E_BUDGET) */
     uint32_t max_admit_per_step;  /* 0 = no limit */
     int use_graphs;               /* replay captured steps while the resident set is stable */
@@ -351,7 +351,7 @@ typedef struct fg_server_config {
                                      predicted device time of one step over the resident scenes
                                      stays within it (an empty server admits any request); the
                                      prediction is a fixed 0.1 ms plus a per-particle rate learned
-                                     from the finished steps; 0 = no time budget (default 0.9) */
+                                     from the finished steps; 0 = no time budget (default 1.1) */
     float head_wait_s;            /* once the oldest queued request has waited this long and does
                                      not fit, it gets a reservation: a younger request is admitted
                                      only if it fits now and finishes before enough resident scenes

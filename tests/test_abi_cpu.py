@@ -196,5 +196,5 @@ def test_server_config_defaults(lib):
     c = _ffi.fg_server_config()
     lib.fg_server_config_defaults(ctypes.byref(c))
     assert c.hbm_budget_bytes == 120 << 30 and c.use_graphs == 1
-    assert c.max_particles == 850000 and c.target_step_ms == pytest.approx(0.9)
+    assert c.max_particles == 1200000 and c.target_step_ms == pytest.approx(1.1)
     assert c.head_wait_s == 0.0 and c.pipeline_depth == 0
