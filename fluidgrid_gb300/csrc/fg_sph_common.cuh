@@ -205,6 +205,12 @@ __device__ __forceinline__ float cc_sum(float v)
     return v;
 }
 
+/* widest search half-width whose bucket rows the contact walk loads together */
+#define FG_CONTACT_ROW_MAX 2
+#ifndef FG_CONTACT_ROWS
+#define FG_CONTACT_ROWS 1
+#endif
+
 /* Rigid-sphere contact of one fluid particle against a rigid grid
  * (ProcessCollisionForcesD with the per-body velocity of w, eps from the
  * scene).  Skipped when the particle is outside the scene's sphere AABB
@@ -225,6 +231,50 @@ __device__ __forceinline__ float3 fg_fluid_rigid_contact(const FgScene *S, uint3
     const float3 P = make_float3(p.x, p.y, p.z);
     const float3 V = make_float3(v.x, v.y, v.z);
     const int rx = S->f2r_rel[0], ry = S->f2r_rel[1], rz = S->f2r_rel[2];
+    auto bucket = [&](uint32_t hx, uint32_t hy, uint32_t hz) {
+        return G.own_geometry ? fg_bucket(hx, hy, hz, G.nb, G.mask)
+                              : S->rb_bucket_base + fg_bucket(hx, hy, hz, S->rb_nb, S->rb_nb_mask);
+    };
+    auto visit = [&](uint32_t st, uint32_t en) {
+        for (uint32_t j = st; j < en; j++) {
+            const float4 q = __ldg(G.spos + j);
+            const float4 vq = dynamic ? __ldg(G.body_vel + (int)q.w) : make_float4(0.f, 0.f, 0.f, 0.f);
+            fg_contact(acc, P, V, q, vq, mind, S->ck, S->ckd);
+        }
+    };
+#if FG_CONTACT_ROWS
+    if (rx >= 0 && rx <= FG_CONTACT_ROW_MAX) {
+        /* the same buckets in the same order, with the x hashes computed
+         * once and each x row's bucket ranges loaded together: a particle
+         * near a body pays one memory latency per row instead of one per
+         * bucket (125 buckets at the default half-width of 2) */
+        uint32_t hx[2 * FG_CONTACT_ROW_MAX + 1];
+#pragma unroll
+        for (int k = 0; k <= 2 * FG_CONTACT_ROW_MAX; k++)
+            hx[k] = k <= 2 * rx ? fg_axis_hash_rel(p.x, S->rb_cell[0], k - rx, FG_PX) : 0u;
+        for (int z = -rz; z <= rz; z++) {
+            const uint32_t hz = fg_axis_hash_rel(p.z, S->rb_cell[2], z, FG_PZ);
+            for (int y = -ry; y <= ry; y++) {
+                const uint32_t hy = fg_axis_hash_rel(p.y, S->rb_cell[1], y, FG_PY);
+                uint32_t st[2 * FG_CONTACT_ROW_MAX + 1], en[2 * FG_CONTACT_ROW_MAX + 1];
+#pragma unroll
+                for (int k = 0; k <= 2 * FG_CONTACT_ROW_MAX; k++) {
+                    st[k] = FG_EMPTY;
+                    en[k] = 0u;
+                    if (k <= 2 * rx) {
+                        const uint32_t b = bucket(hx[k], hy, hz);
+                        st[k] = __ldg(G.start + b);
+                        en[k] = __ldg(G.end + b);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k <= 2 * FG_CONTACT_ROW_MAX; k++)
+                    if (st[k] != FG_EMPTY) visit(st[k], en[k]);
+            }
+        }
+        return acc;
+    }
+#endif
     for (int z = -rz; z <= rz; z++) {
         const uint32_t hz = fg_axis_hash_rel(p.z, S->rb_cell[2], z, FG_PZ);
         for (int y = -ry; y <= ry; y++) {
