@@ -92,6 +92,7 @@ World::~World()
     if (ev_bodies_done) cudaEventDestroy(ev_bodies_done);
     if (ev_io_fork) cudaEventDestroy(ev_io_fork);
     if (ev_vel_in) cudaEventDestroy(ev_vel_in);
+    if (ev_pos_in) cudaEventDestroy(ev_pos_in);
     if (stream2) cudaStreamDestroy(stream2);
     if (stream3) cudaStreamDestroy(stream3);
     if (own_stream && stream) cudaStreamDestroy(stream);
@@ -245,6 +246,7 @@ size_t World::footprint(const Capacity &c, uint32_t list_cap)
     b += (sizeof(FgScene) + 24) * std::max<uint64_t>(c.scenes, 1);
     b += sizeof(FgWork) * (std::max<uint64_t>(c.work, 1) + std::max<uint64_t>(c.work_sph, 1));
     if (c.bodies) {
+        b += P * 16; /* the fluid side of the contact */
         b += S * (16 * 6 + 12);
         b += 8 * std::max<uint64_t>(c.rb_buckets, 1);
         b += c.bodies * (32 * 6 + 16 * 3 + 8 + 72 + 12 + 8 * 8 * FG_BODY_CHUNKS);
@@ -311,6 +313,7 @@ int World::reserve(const Capacity &c)
     if (c.bodies) {
         const size_t S = std::max<uint64_t>(c.spheres, 1), B = c.bodies;
         const size_t RB = std::max<uint64_t>(c.rb_buckets, 1);
+        if ((r = A((void **)&fcontact, 16 * N))) return r;
         if ((r = A((void **)&rb_local, 16 * S))) return r;
         if ((r = A((void **)&rb_world, 16 * S))) return r;
         if ((r = A((void **)&rb_keys_u, 4 * S))) return r;
@@ -539,6 +542,7 @@ int World::init_stream(cudaStream_t st)
     CK(cudaStreamCreateWithFlags(&stream3, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&ev_io_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_vel_in, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_pos_in, cudaEventDisableTiming));
     return FG_OK;
 }
 
@@ -625,7 +629,28 @@ void World::enqueue_rb_grid(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches
 
 /* Sphere forces and torques from the fluid (and from other bodies) (the
  * stage bit FG_STAGE_RB_CONTACT). */
-void World::enqueue_rb_contact(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches)
+/* The bodies' rigid-sphere grid as the fluid side of the contact reads it. */
+RigidGrid World::body_grid() const
+{
+    RigidGrid G;
+    memset(&G, 0, sizeof(G));
+    G.spos = rb_spos;
+    G.start = rb_start;
+    G.end = rb_end;
+    G.body_vel = bvf;
+    G.aabb = aabb;
+    return G;
+}
+
+/* Whether a whole step computes the fluid side of the contact in its own
+ * pass (with the sphere side, beside the density pass) for the force pass to
+ * read; kernel 2's force pass walks the rigid grid itself. */
+bool World::fluid_contact_pass() const
+{
+    return nbodies > 0 && fcontact && !use_cc && (stages & FG_STAGE_RB_CONTACT);
+}
+
+void World::enqueue_rb_contact(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches, bool with_fluid)
 {
     if (!(stages & FG_STAGE_RB_CONTACT)) return;
     if (ev) cudaEventRecord(ev[10], st);
@@ -637,7 +662,19 @@ void World::enqueue_rb_contact(cudaStream_t st, cudaEvent_t *ev, uint32_t &launc
         launch_rb_from_rb(Ls, rb_spos, rb_ids, bvf, bxf, rb_start, rb_end, rb_force, rb_torque, nullptr, 1);
         launches++;
     }
+    if (with_fluid) enqueue_fluid_contact(st, launches);
     if (ev) cudaEventRecord(ev[11], st);
+}
+
+/* The fluid side of the contact (by particle id, from the step's unsorted
+ * state and the bodies' sphere grid) for the force pass to read. */
+void World::enqueue_fluid_contact(cudaStream_t st, uint32_t &launches)
+{
+    if (!fluid_contact_pass()) return;
+    Launch Lf = fluid_launch();
+    Lf.stream = st;
+    launch_fluid_contact(Lf, pos, vel, body_grid(), fcontact);
+    launches++;
 }
 
 #define CK0(call)                                                                                  \
@@ -739,6 +776,17 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
         CK0(cudaEventRecord(ev_vel_in, stream3));
         CK0(cudaMemcpyAsync(pos, cur_io->hp, iob, cudaMemcpyHostToDevice, stream));
     }
+    if (fork) {
+        /* the fluid side of the contact follows the sphere grid on the second
+         * stream, beside the hash and sort; an end-to-end step's pass waits
+         * for the state's upload */
+        if (cur_io && iob && fluid_contact_pass()) {
+            CK0(cudaEventRecord(ev_pos_in, stream));
+            CK0(cudaStreamWaitEvent(stream2, ev_pos_in, 0));
+            CK0(cudaStreamWaitEvent(stream2, ev_vel_in, 0));
+        }
+        enqueue_fluid_contact(stream2, launches);
+    }
     counted_in_hash = false;
     if (stages & FG_STAGE_HASH) {
         mark(0, 0);
@@ -779,7 +827,7 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
     if (fork) {
         CK0(cudaEventRecord(ev_fluid_ready, stream));
         CK0(cudaStreamWaitEvent(stream2, ev_fluid_ready, 0));
-        enqueue_rb_contact(stream2, nullptr, launches);
+        enqueue_rb_contact(stream2, nullptr, launches, false);
         CK0(cudaEventRecord(ev_rb_done, stream2));
         if (fork_bodies) {
             enqueue_bodies(stream2, bvf_next);
@@ -800,20 +848,14 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
     }
     if (rb && !fork) {
         enqueue_rb_grid(stream, ev, launches);
-        enqueue_rb_contact(stream, ev, launches);
+        enqueue_rb_contact(stream, ev, launches, true);
     }
     if (fork) CK0(cudaStreamWaitEvent(stream, ev_rb_done, 0));
     if (stages & FG_STAGE_FORCES) {
         mark(6, 0);
-        RigidGrid G;
-        G.spos = rb_spos;
-        G.start = rb_start;
-        G.end = rb_end;
-        G.body_vel = bvf;
-        G.aabb = aabb;
-        G.own_geometry = 0;
-        G.nb = 0;
-        G.mask = 0;
+        RigidGrid G = body_grid();
+        /* the fluid side of the contact ran as its own pass (enqueue_fluid_contact) */
+        if (fluid_contact_pass()) G.pre = fcontact;
         ForceOut o;
         o.vel = vel;
         o.pos = fused_integrate ? pos : nullptr;
@@ -1233,15 +1275,7 @@ int World::run_stage(int stage, int flags)
             set_error_msg("FG_RUN_FORCES reads the bodies' old velocities: run it before FG_RUN_BODY_INTEGRATE");
             return FG_E_STATE;
         }
-        RigidGrid G;
-        G.spos = rb_spos;
-        G.start = rb_start;
-        G.end = rb_end;
-        G.body_vel = bvf;
-        G.aabb = aabb;
-        G.own_geometry = 0;
-        G.nb = 0;
-        G.mask = 0;
+        const RigidGrid G = body_grid();
         ForceOut o;
         o.vel = vel;
         o.pos = nullptr; /* FG_RUN_INTEGRATE moves the particles */
@@ -1316,7 +1350,7 @@ uint32_t World::launches_per_step()
     if (nbodies) {
         if (stages & FG_STAGE_RB_GRID) /* aabb reset, hash, sort + ranges */
             c += rb_small_scenes ? 3 : 3 + 3 * radix_passes(rb_key_bits, 8);
-        if (stages & FG_STAGE_RB_CONTACT) c += 1 + (any_rb_rb ? 1 : 0);
+        if (stages & FG_STAGE_RB_CONTACT) c += 1 + (any_rb_rb ? 1 : 0) + (fluid_contact_pass() ? 1 : 0);
         if (stages & FG_STAGE_BODIES) c += body_launches();
     }
     if (stages & FG_STAGE_FORCES) c += fused_integrate ? 1 : 2;

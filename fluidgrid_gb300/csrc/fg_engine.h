@@ -101,6 +101,7 @@ struct World {
     }
     /* rigid */
     float4 *rb_local = nullptr, *rb_world = nullptr, *rb_spos = nullptr, *rb_force = nullptr, *rb_torque = nullptr;
+    float4 *fcontact = nullptr; /* per sorted fluid particle: its contact with the bodies' spheres */
     uint32_t *rb_keys_u = nullptr, *rb_keys = nullptr, *rb_ids = nullptr, *rb_start = nullptr, *rb_end = nullptr;
     int *aabb = nullptr;
     FgD4 *bx = nullptr, *bv = nullptr, *bq = nullptr, *bL = nullptr, *bfs = nullptr, *bts = nullptr;
@@ -118,9 +119,12 @@ struct World {
     cudaStream_t stream2 = nullptr; /* rigid-body branch of a full step */
     cudaEvent_t ev_fork = nullptr, ev_fluid_ready = nullptr, ev_rb_done = nullptr, ev_bodies_done = nullptr;
     cudaStream_t stream3 = nullptr; /* velocity upload of an end-to-end step */
-    cudaEvent_t ev_io_fork = nullptr, ev_vel_in = nullptr;
+    cudaEvent_t ev_io_fork = nullptr, ev_vel_in = nullptr, ev_pos_in = nullptr;
     void enqueue_rb_grid(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches);
-    void enqueue_rb_contact(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches);
+    void enqueue_rb_contact(cudaStream_t st, cudaEvent_t *ev, uint32_t &launches, bool with_fluid);
+    void enqueue_fluid_contact(cudaStream_t st, uint32_t &launches);
+    RigidGrid body_grid() const;
+    bool fluid_contact_pass() const;
     void enqueue_bodies(cudaStream_t st, float4 *vf);
     /* kernels of one body update: the chunked FP64 partial sums (up to 65,535
      * bodies) and the update */

@@ -144,6 +144,10 @@ struct RigidGrid {
     const int *aabb;        /* per scene ordered-int AABB of sphere centres, or null */
     int own_geometry;       /* 1: bucket count below (bucket base 0); 0: the scene's rigid grid */
     uint32_t nb, mask;
+    /* the force pass: each fluid particle's contact with this grid, by
+     * particle id, written by launch_fluid_contact for the particles inside
+     * the bodies' grown AABB; null = the force pass walks the grid itself */
+    const float4 *pre;
 };
 
 struct ForceOut {
@@ -155,6 +159,13 @@ void launch_forces(const Launch &L, const float4 *spos, const float4 *svel, cons
                    const uint32_t *end, const uint32_t *ids, ForceOut out, const RigidGrid *rigid,
                    const RigidGrid *statics, float mass_override, float visc_override, int use_override,
                    const NbrList *list = nullptr, TargetOrder ord = TargetOrder{nullptr, nullptr});
+
+/* The fluid side of the fluid/rigid contact as its own pass, over the
+ * unsorted particles: for every active fluid particle of a scene with bodies
+ * that lies inside the bodies' AABB grown by the contact distance, out[id] =
+ * its contact with grid G (ProcessCollisionForcesD).  The force pass then
+ * reads it (G.pre). */
+void launch_fluid_contact(const Launch &L, const float4 *pos, const float4 *vel, const RigidGrid &G, float4 *out);
 
 void launch_integrate(const Launch &L, float4 *pos, const float4 *vel);
 

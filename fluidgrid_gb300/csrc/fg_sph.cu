@@ -272,7 +272,13 @@ __global__ void __launch_bounds__(BLOCK, 768 / BLOCK) k_forces(const FgWork *__r
                 F.x += c.x; F.y += c.y; F.z += c.z;
             }
             if (R.use_dyn && (S->flags & FG_SCENE_HAS_RB)) {
-                float3 c = fg_fluid_rigid_contact(S, it.scene, p, v, R.dyn, true);
+                float3 c = make_float3(0.f, 0.f, 0.f);
+                if (!R.dyn.pre) {
+                    c = fg_fluid_rigid_contact(S, it.scene, p, v, R.dyn, true);
+                } else if (!fg_contact_outside(S, it.scene, p, R.dyn)) {
+                    const float4 q = R.dyn.pre[ord.tord ? pid : __ldg(ids + i)];
+                    c = make_float3(q.x, q.y, q.z);
+                }
                 F.x += c.x; F.y += c.y; F.z += c.z;
             }
             const float3 wl = fg_walls(*S, make_float3(p.x, p.y, p.z), make_float3(v.x, v.y, v.z));
@@ -333,6 +339,41 @@ void launch_forces(const Launch &L, const float4 *spos, const float4 *svel, cons
         if (list) FG_FORCES(true, 128); else FG_FORCES(false, 128);
     }
 #undef FG_FORCES
+}
+
+/* The fluid side of the fluid/rigid contact ahead of the force pass, by
+ * particle id from the step's unsorted positions and velocities (the sorted
+ * copies hold the same bits), so it runs right after the rigid-sphere grid
+ * beside the fluid hash and sort.  Inside the force pass, the few particles
+ * near a body walked (2r+1)^3 rigid buckets while the rest of their warps and
+ * CTAs waited at 80 registers a thread.  The force pass adds the stored sum
+ * where it added the walked one: the same bits. */
+__global__ void __launch_bounds__(FG_CHUNK) k_fluid_contact(const FgWork *__restrict__ work, uint32_t nwork,
+                                                           uint32_t n_single, const FgScene *__restrict__ table,
+                                                           const __grid_constant__ FgScene single,
+                                                           const float4 *__restrict__ pos,
+                                                           const float4 *__restrict__ vel,
+                                                           const __grid_constant__ RigidGrid G,
+                                                           float4 *__restrict__ out)
+{
+    for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const FgWork it = fg_work(work, w, n_single);
+        if (threadIdx.x >= it.count) continue;
+        const FgScene *S = fg_scene(table, &single, it.scene);
+        if (!(S->flags & FG_SCENE_HAS_RB)) continue;
+        const uint32_t id = it.first + threadIdx.x;
+        const float4 p = pos[id];
+        if (!(p.w > 0.0f) || fg_contact_outside(S, it.scene, p, G)) continue;
+        const float3 c = fg_fluid_rigid_contact(S, it.scene, p, vel[id], G, true);
+        out[id] = make_float4(c.x, c.y, c.z, 0.0f);
+    }
+}
+
+void launch_fluid_contact(const Launch &L, const float4 *pos, const float4 *vel, const RigidGrid &G, float4 *out)
+{
+    if (!L.nwork) return;
+    k_fluid_contact<<<grid_for(L.nwork, 16), FG_CHUNK, 0, L.stream>>>(L.work, L.nwork, L.n, L.table, *L.single, pos,
+                                                                     vel, G, out);
 }
 
 /* SPHIntegrateK (K_FluidSim.cu:418-438): pos += vel*(dt/scale) for active

@@ -211,23 +211,29 @@ __device__ __forceinline__ float cc_sum(float v)
 #define FG_CONTACT_ROWS 1
 #endif
 
+/* Whether a fluid particle lies outside the bodies' AABB of its scene grown
+ * by the contact distance: its contact sum is then exactly zero. */
 /* Rigid-sphere contact of one fluid particle against a rigid grid
  * (ProcessCollisionForcesD with the per-body velocity of w, eps from the
  * scene).  Skipped when the particle is outside the scene's sphere AABB
  * grown by the contact distance: there every candidate is out of range, so
  * the sum is exactly zero as in the reference. */
+__device__ __forceinline__ bool fg_contact_outside(const FgScene *S, uint32_t scene, float4 p, const RigidGrid &G)
+{
+    if (!G.aabb) return false;
+    const float mind = S->fluid_radius + S->rb_radius + S->fluid_eps;
+    const int *bx = G.aabb + 6 * scene;
+    return p.x < fg_ord_float(bx[0]) - mind || p.y < fg_ord_float(bx[1]) - mind ||
+           p.z < fg_ord_float(bx[2]) - mind || p.x > fg_ord_float(bx[3]) + mind ||
+           p.y > fg_ord_float(bx[4]) + mind || p.z > fg_ord_float(bx[5]) + mind;
+}
+
 __device__ __forceinline__ float3 fg_fluid_rigid_contact(const FgScene *S, uint32_t scene, float4 p, float4 v,
                                                          const RigidGrid &G, bool dynamic)
 {
     float3 acc = make_float3(0.f, 0.f, 0.f);
     const float mind = S->fluid_radius + S->rb_radius + S->fluid_eps;
-    if (G.aabb) {
-        const int *bx = G.aabb + 6 * scene;
-        if (p.x < fg_ord_float(bx[0]) - mind || p.y < fg_ord_float(bx[1]) - mind ||
-            p.z < fg_ord_float(bx[2]) - mind || p.x > fg_ord_float(bx[3]) + mind ||
-            p.y > fg_ord_float(bx[4]) + mind || p.z > fg_ord_float(bx[5]) + mind)
-            return acc;
-    }
+    if (fg_contact_outside(S, scene, p, G)) return acc;
     const float3 P = make_float3(p.x, p.y, p.z);
     const float3 V = make_float3(v.x, v.y, v.z);
     const int rx = S->f2r_rel[0], ry = S->f2r_rel[1], rz = S->f2r_rel[2];
