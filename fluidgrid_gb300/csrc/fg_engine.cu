@@ -842,7 +842,7 @@ uint32_t World::enqueue_step(cudaEvent_t *ev)
                               end, dp, nbr.rec, n, stream, cc_warps);
         else
             launch_density(L, spos, start, end, dp, 0.f, 0.f, 0.f, 0, svel, use_list ? &nbr : nullptr,
-                           target_order(), pair_counter);
+                           density_order(), pair_counter);
         mark(3, 1);
         launches++;
     }
@@ -904,11 +904,14 @@ void World::enqueue_order_refresh()
 
 uint64_t World::graph_signature() const
 {
-    return (uint64_t)((stages & 0xffu) | (fused_integrate ? 0x100u : 0u) | (digit_bits << 9) |
-                      (use_list ? 0x10000u : 0u) | ((use_order && order_valid) ? 0x20000u : 0u) |
-                      (use_cc ? 0x40000u : 0u) | ((ctas_per_sm & 0x7fu) << 20) |
-                      (one_pass_sort ? 0x8000000u : 0u) | (bucket_sort_on ? 0x10000000u : 0u) | ((block >> 6) << 28) | ((cc_warps & 0x7u) << 24)) |
-           ((uint64_t)nbr.stride << 32);
+    /* every setting that changes the captured launches, each in its own bits */
+    const bool ordered = use_order && order_valid;
+    return (uint64_t)(stages & 0xffu) | (fused_integrate ? 0x100ull : 0ull) | ((uint64_t)(digit_bits & 0xfu) << 9) |
+           (use_list ? 1ull << 16 : 0ull) | (ordered ? 1ull << 17 : 0ull) | (use_cc ? 1ull << 18 : 0ull) |
+           ((ordered && order_forces_only) ? 1ull << 19 : 0ull) | ((uint64_t)(ctas_per_sm & 0x7fu) << 20) |
+           (one_pass_sort ? 1ull << 27 : 0ull) | (bucket_sort_on ? 1ull << 28 : 0ull) |
+           ((uint64_t)((block >> 6) & 0x7u) << 29) | ((uint64_t)(cc_warps & 0x7u) << 32) |
+           ((uint64_t)nbr.stride << 40);
 }
 
 /* The capacity is a device word the kernels read, so changing it within the
@@ -1099,12 +1102,20 @@ int World::check_list_cap()
     return set_list_cap(want);
 }
 
+/* Whether step s starts by refreshing the Morton target order. */
+bool World::order_refresh_due(uint64_t s) const
+{
+    return use_order && !needs_runs() && (stages & FG_STAGE_DENSITY) &&
+           (!order_valid || (order_period && s % order_period == 0));
+}
+
 /* Steps at which the host acts between steps (autotuning rounds, list
  * capacity checks): a multi-step graph never spans one. */
 bool World::host_boundary(uint64_t s) const
 {
     if (tune_period && s % tune_period == 0) return true;
     if (use_list && list_autogrow && s % FG_LIST_CHECK_PERIOD == 0) return true;
+    if (order_refresh_due(s)) return true;
     return false;
 }
 
@@ -1123,7 +1134,7 @@ int World::step(uint32_t nsteps, const StepIO *io)
 int World::step_loop(uint32_t nsteps)
 {
     for (uint32_t k = 0; k < nsteps; k++) {
-        if (use_graphs && graph_steps > 1 && !cur_io && !tr.active && !use_order && nsteps - k >= graph_steps &&
+        if (use_graphs && graph_steps > 1 && !cur_io && !tr.active && nsteps - k >= graph_steps &&
             !host_boundary(step_count)) {
             bool clear = true;
             for (uint32_t q = 1; q < graph_steps && clear; q++) clear = !host_boundary(step_count + q);
@@ -1144,10 +1155,8 @@ int World::step_loop(uint32_t nsteps)
             int r = check_list_cap();
             if (r != FG_OK) return r;
         }
-        if (!tr.active && tune_period && !use_order && (step_count % tune_period == 0)) tune_begin();
-        const bool refresh = use_order && !needs_runs() && (stages & FG_STAGE_DENSITY) &&
-                             (!order_valid || (order_period && step_count % order_period == 0));
-        if (refresh) enqueue_order_refresh();
+        if (!tr.active && tune_period && (step_count % tune_period == 0)) tune_begin();
+        if (order_refresh_due(step_count)) enqueue_order_refresh();
         if (tr.active) tune_apply(tr.dim, tr.cand[tr.idx]);
         const int kused = current_kernel();
         /* the graph is found (or captured and instantiated) before a trial's
@@ -1213,8 +1222,7 @@ int World::run_stage(int stage, int flags)
             int r = check_list_cap();
             if (r != FG_OK) return r;
         }
-        if (use_order && !needs_runs() && (!order_valid || (order_period && step_count % order_period == 0)))
-            enqueue_order_refresh();
+        if (order_refresh_due(step_count)) enqueue_order_refresh();
         enqueue_hash(L, true);
         counted_ranges = fused_ranges = false;
         enqueue_sort(true);
@@ -1236,7 +1244,7 @@ int World::run_stage(int stage, int flags)
                               end, dp, nbr.rec, n, stream, cc_warps);
         else
             launch_density(L, spos, start, end, dp, 0.f, 0.f, 0.f, 0, svel, use_list ? &nbr : nullptr,
-                           target_order(), pair_counter);
+                           density_order(), pair_counter);
         break;
     case FG_RUN_RB_GRID: {
         if (!rb) break;
@@ -1837,7 +1845,11 @@ int fg_world_set_option(fg_world *w, int option, int value)
     World *W = (World *)w;
     switch (option) {
     case FG_OPT_NEIGHBOR_LIST: W->use_list = value != 0; return FG_OK;
-    case FG_OPT_TARGET_ORDER: W->use_order = value != 0; return FG_OK;
+    case FG_OPT_TARGET_ORDER:
+        if (value < 0 || value > 2) return FG_E_INVALID;
+        W->use_order = value != 0;
+        W->order_forces_only = value == 2;
+        return FG_OK;
     case FG_OPT_ORDER_PERIOD:
         if (value < 0) return FG_E_INVALID;
         W->order_period = (uint32_t)value;
@@ -1939,7 +1951,7 @@ int fg_world_get_option(const fg_world *w, int option, int *value)
     const World *W = (const World *)w;
     switch (option) {
     case FG_OPT_NEIGHBOR_LIST: *value = W->use_list ? 1 : 0; return FG_OK;
-    case FG_OPT_TARGET_ORDER: *value = W->use_order ? 1 : 0; return FG_OK;
+    case FG_OPT_TARGET_ORDER: *value = W->use_order ? (W->order_forces_only ? 2 : 1) : 0; return FG_OK;
     case FG_OPT_ORDER_PERIOD: *value = (int)W->order_period; return FG_OK;
     case FG_OPT_DIGIT_BITS: *value = (int)W->digit_bits; return FG_OK;
     case FG_OPT_KERNEL: *value = W->current_kernel(); return FG_OK;

@@ -83,7 +83,9 @@ struct World {
     uint32_t *list_cap_d = nullptr; /* the same, in device memory for the kernels */
     uint32_t *inv = nullptr;  /* particle -> sorted index (written by the ranges pass) */
     uint32_t *tord = nullptr; /* spatial target order (particle ids, scene-contiguous) */
-    bool use_list = true, use_order = false;
+    /* default: Morton target order in the force pass only (FG_OPT_TARGET_ORDER 2) */
+    bool use_list = true, use_order = true;
+    bool order_forces_only = true;
     bool use_cc = false;       /* kernel 2: warp per bucket run, candidates staged in shared memory */
     uint32_t ctas_per_sm = 0;  /* CTAs per SM of the density/force grids (0 = 64) */
     uint32_t block = 128;      /* kernels 0/1: threads per CTA of the density/force grids (64, 128, 256) */
@@ -95,10 +97,18 @@ struct World {
     uint64_t step_count = 0;
     bool order_valid = false;
     void enqueue_order_refresh();
+    /* the target order of the force pass, and of the density pass unless
+     * the Morton order is the force pass's only; the neighbour lists are
+     * indexed by sorted particle, so the two passes may differ */
     TargetOrder target_order() const
     {
         return (use_order && order_valid) ? TargetOrder{tord, inv} : TargetOrder{nullptr, nullptr};
     }
+    TargetOrder density_order() const
+    {
+        return order_forces_only ? TargetOrder{nullptr, nullptr} : target_order();
+    }
+    bool order_refresh_due(uint64_t s) const;
     /* rigid */
     float4 *rb_local = nullptr, *rb_world = nullptr, *rb_spos = nullptr, *rb_force = nullptr, *rb_torque = nullptr;
     float4 *fcontact = nullptr; /* per sorted fluid particle: its contact with the bodies' spheres */

@@ -80,7 +80,8 @@ __global__ void __launch_bounds__(BLOCK, 2048 / BLOCK) k_density(const FgWork *_
         const bool active = valid && p.w > 0.0f; /* inactive: density not written */
         DensityAcc acc;
         acc.init();
-        uint32_t *lp = LIST ? list.idx + (size_t)tpos * list.stride : nullptr;
+        /* lists by sorted index: the force pass may visit the targets in another order */
+        uint32_t *lp = LIST ? list.idx + (size_t)i * list.stride : nullptr;
         if (active) {
             const float scale = S->scale, h2 = S->h2;
             const float px = p.x * scale, py = p.y * scale, pz = p.z * scale;
@@ -107,7 +108,7 @@ __global__ void __launch_bounds__(BLOCK, 2048 / BLOCK) k_density(const FgWork *_
             list.rec[2 * i + 1] = make_float4(v.x, v.y, v.z, d.y);
         }
         const uint32_t cnt = acc.cnt, dcnt = LIST ? acc.cnt : acc.dcnt;
-        if (LIST && valid) list.cnt[tpos] = cnt;
+        if (LIST && valid) list.cnt[i] = cnt;
         pc += dcnt;
         mx = max(mx, cnt);
         ovf += (LIST && cnt > cap) ? 1u : 0u;
@@ -202,11 +203,11 @@ __global__ void __launch_bounds__(BLOCK, 768 / BLOCK) k_forces(const FgWork *__r
             if (LIST) {
                 const float4 r0 = list.rec[2 * i], r1 = list.rec[2 * i + 1];
                 const float rho_i = r0.w, P_i = r1.w;
-                const uint32_t c = list.cnt[tpos];
+                const uint32_t c = list.cnt[i];
                 if (c <= __ldg(list.cap)) {
                     /* in-range visits in walk order (the target's own
                      * entries skipped) */
-                    const uint32_t *nl = list.idx + (size_t)tpos * list.stride;
+                    const uint32_t *nl = list.idx + (size_t)i * list.stride;
                     /* the list is padded with i to whole groups of four */
                     const uint32_t c4 = (c + 3u) & ~3u;
                     /* four 32-byte records in flight, one 256-bit load each,

@@ -186,7 +186,11 @@ int fg_world_set_graphs(fg_world *w, int on);
  *                         2 = one warp per run, one target at a time
  *   FG_OPT_NEIGHBOR_LIST  1 = kernel 1, 0 = kernel 0
  *   FG_OPT_TARGET_ORDER   kernels 0/1: 1 = targets in Morton order of their
- *                         cells, 0 = hashed bucket order (default)
+ *                         cells, 0 = hashed bucket order, 2 = Morton order in
+ *                         the force pass only (default; server worlds 0): the
+ *                         density pass walks in bucket order, where a warp's
+ *                         lanes share their buckets, and the force pass's
+ *                         lanes, spatially close, share neighbour records
  *   FG_OPT_ORDER_PERIOD   steps between refreshes of the Morton order (16)
  *   FG_OPT_DIGIT_BITS     radix digit width 1..8
  *   FG_OPT_AUTOTUNE_PERIOD  every this many steps the autotuner runs one

@@ -163,12 +163,12 @@ def test_fused_equals_separate_and_graph_equals_direct():
 @pytest.mark.parametrize("name", ["dam_break_16k", "far_origin"])
 def test_tunables_do_not_change_results(name):
     """The per-particle kernels (walk or neighbour lists, bucket or Morton
-    target order) only change how the work is scheduled: every setting
-    evolves the state bit-identically."""
+    target order in both passes or in the force pass only) only change how
+    the work is scheduled: every setting evolves the state bit-identically."""
     spec = VARIANTS[name]
     outs = {}
     for kernel in (0, 1):
-        for order in (0, 1):
+        for order in (0, 1, 2):
             for period in ((1, 16) if order else (16,)):
                 w = World([spec])
                 w.set_option("autotune_period", 0)
