@@ -906,9 +906,11 @@ __global__ void __launch_bounds__(FG_CHUNK) k_morton_keys(const FgWork *__restri
         const float q[3] = {p.x, p.y, p.z};
 #pragma unroll
         for (int a = 0; a < 3; a++) {
-            float f = (q[a] - S->vmin[a]) / S->cell[a] + 2.0f;
-            int v = (f > 0.0f) ? (int)fminf(f, (float)lim) : 0;
-            c[a] = v > lim ? lim : v;
+            /* the hash grid's own cell index (relative to the scene's lower
+             * corner): a Morton cell is exactly one hashed cell, so a run of
+             * targets shares its 27 buckets as in bucket order */
+            const int v = fg_axis_index(q[a], S->cell[a]) - fg_axis_index(S->vmin[a], S->cell[a]) + 2;
+            c[a] = v < 0 ? 0 : (v > lim ? lim : v);
         }
         const uint32_t m = (fg_spread3((uint32_t)c[0]) | (fg_spread3((uint32_t)c[1]) << 1) |
                             (fg_spread3((uint32_t)c[2]) << 2));
