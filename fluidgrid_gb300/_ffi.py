@@ -122,7 +122,7 @@ C_ABI_SYMBOLS = [
     "fg_world_check", "fg_world_upload", "fg_world_download", "fg_world_scene_upload", "fg_world_scene_download",
     "fg_world_particles", "fg_world_scenes", "fg_world_spheres", "fg_world_bodies", "fg_world_scene_layout",
     "fg_world_buffer", "fg_world_set_stages", "fg_world_set_fused_integrate", "fg_world_set_sort_digit_bits",
-    "fg_world_set_graphs", "fg_world_launches_per_step", "fg_world_stage_profile", "fg_world_timed_steps",
+    "fg_world_set_graphs", "fg_world_launches_per_step", "fg_world_kernel_launches", "fg_world_stage_profile", "fg_world_timed_steps",
     "fg_world_e2e_steps", "fg_host_alloc", "fg_host_free", "fg_set_device", "fg_probe_fp32_peak",
     "fg_sort_pairs_noalloc", "fg_selftest_bounded_wait", "fg_world_set_option", "fg_world_get_option", "fg_world_tuning_stats",
     "fg_world_counters", "fg_world_list_overflows", "fg_world_timed_blocks", "fg_world_diagnostics", "fg_server_config_defaults", "fg_server_create",
@@ -173,6 +173,7 @@ def load():
               "fg_world_launches_per_step"):
         getattr(L, n).argtypes = [VP]
         getattr(L, n).restype = c_u32
+    L.fg_world_kernel_launches.argtypes = [VP, P(ctypes.c_uint64)]
     L.fg_world_scene_layout.argtypes = [VP, c_u32, P(c_u32)]
     L.fg_world_buffer.argtypes = [VP, ctypes.c_int, P(VP), P(ctypes.c_size_t)]
     L.fg_world_set_stages.argtypes = [VP, c_u32]

@@ -899,6 +899,7 @@ void World::enqueue_order_refresh()
     if (!n) return;
     launch_morton_keys(fluid_launch(), pos, keys, order_bits, order_scene_shift);
     radix_sort(keys, nullptr, keys_u, tord, n, order_key_bits, digit_bits, rs, stream);
+    kernels_enqueued += 1 + 3 * (uint64_t)radix_passes(order_key_bits, digit_bits);
     order_valid = true;
 }
 
@@ -1144,6 +1145,7 @@ int World::step_loop(uint32_t nsteps)
                 int r = graph_for_current(&ge, graph_steps);
                 if (r != FG_OK) return r;
                 CK(cudaGraphLaunch(ge, stream));
+                kernels_enqueued += (uint64_t)graph_steps * launches_per_step();
                 tune_count[current_kernel()] += graph_steps;
                 counted_steps += graph_steps;
                 step_count += graph_steps;
@@ -1170,6 +1172,7 @@ int World::step_loop(uint32_t nsteps)
         if (tr.active) CK(cudaEventRecord(tr.ev[2 * tr.idx], stream));
         if (!use_graphs) enqueue_step();
         else CK(cudaGraphLaunch(ge, stream));
+        kernels_enqueued += launches_per_step();
         if (tr.active) {
             CK(cudaEventRecord(tr.ev[2 * tr.idx + 1], stream));
             if (++tr.idx == tr.ncand) {
@@ -1458,7 +1461,7 @@ int World::stage_profile(size_t fbytes, float *ms)
     }
     for (int k = 0; k < 8; k++) ms[k] = 0.0f;
     if (use_order && !order_valid) enqueue_order_refresh();
-    enqueue_step(E.ev.data());
+    kernels_enqueued += enqueue_step(E.ev.data());
     step_count++;
     counted_steps++;
     tune_count[current_kernel()]++;
@@ -1483,7 +1486,10 @@ int World::timed_steps(uint32_t nsteps, size_t fbytes, float *ms, uint32_t per_b
     }
     Events E(2 * (size_t)nsteps);
     for (uint32_t k = 0; k < nsteps; k++) {
-        if (fbytes) launch_fill(flush_buf, fbytes / 4, k, stream);
+        if (fbytes) {
+            launch_fill(flush_buf, fbytes / 4, k, stream);
+            kernels_enqueued++;
+        }
         CK(cudaEventRecord(E.ev[2 * k], stream));
         int r = step(per_block);
         if (r != FG_OK) return r;
@@ -1967,6 +1973,13 @@ int fg_world_get_option(const fg_world *w, int option, int *value)
     case FG_OPT_AUTOTUNE_TILES: *value = (int)W->tune_tiles; return FG_OK;
     default: return FG_E_INVALID;
     }
+}
+
+int fg_world_kernel_launches(const fg_world *w, uint64_t *count)
+{
+    if (!w || !count) return FG_E_INVALID;
+    *count = ((const World *)w)->kernels_enqueued;
+    return FG_OK;
 }
 
 uint32_t fg_world_launches_per_step(const fg_world *w)

@@ -95,6 +95,7 @@ struct World {
     uint32_t *nruns = nullptr; /* device counter */
     uint32_t order_period = 16, order_bits = 8, order_scene_shift = 24, order_key_bits = 24;
     uint64_t step_count = 0;
+    uint64_t kernels_enqueued = 0; /* kernel launches enqueued or replayed so far */
     bool order_valid = false;
     void enqueue_order_refresh();
     /* the target order of the force pass, and of the density pass unless

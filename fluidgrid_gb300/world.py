@@ -150,6 +150,12 @@ class World:
     def launches_per_step(self):
         return int(self.L.fg_world_launches_per_step(self.h))
 
+    def kernel_launches(self):
+        """Kernel launches this world has enqueued or replayed so far."""
+        c = ctypes.c_uint64(0)
+        check(self.L.fg_world_kernel_launches(self.h, ctypes.byref(c)), "fg_world_kernel_launches")
+        return int(c.value)
+
     # ---------------------------------------------------------------- timing
     STAGES = ["hash", "sort", "ranges", "density", "rb_grid", "rb_contact", "forces", "bodies"]
 

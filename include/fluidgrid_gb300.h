@@ -261,6 +261,9 @@ int fg_world_tuning_stats(const fg_world *w, uint32_t steps_per_kernel[FG_NUM_KE
 
 /* number of kernel launches one step enqueues */
 uint32_t fg_world_launches_per_step(const fg_world *w);
+/* kernel launches this world has enqueued or replayed so far: every step's,
+ * the target-order refreshes and the L2 flushes of fg_world_timed_steps */
+int fg_world_kernel_launches(const fg_world *w, uint64_t *count);
 
 /* ---- measurement (CUDA events on the world's stream) ----
  * One step in direct-launch mode with an event pair around each stage,

@@ -150,6 +150,34 @@ def test_integrate_bit_exact_given_velocity():
         assert np.array_equal(g["POS"].view(np.uint32), ref.view(np.uint32)), fused
 
 
+def test_kernel_launch_count():
+    """The world counts the kernels it enqueues or replays: each step's
+    launches, the target-order refreshes and the timed steps' L2 flushes."""
+    spec = VARIANTS["dam_break_16k"]
+    w = World([spec])
+    w.set_option("autotune_period", 0)
+    w.set_option("target_order", 0)
+    lps = w.launches_per_step()
+    k0 = w.kernel_launches()
+    w.step(7)
+    assert w.kernel_launches() - k0 == 7 * lps
+    k0 = w.kernel_launches()
+    w.timed_steps(3, 1 << 20)
+    assert w.kernel_launches() - k0 == 3 * (lps + 1)
+    w.close()
+    w = World([spec])
+    w.set_option("autotune_period", 0)
+    w.set_option("target_order", 2)
+    w.set_option("order_period", 16)
+    k0 = w.kernel_launches()
+    w.step(16)  # one refresh, at the first step
+    d16 = w.kernel_launches() - k0
+    w.step(16)  # one more
+    assert d16 > 16 * w.launches_per_step()
+    assert w.kernel_launches() - k0 == 2 * d16
+    w.close()
+
+
 def test_fused_equals_separate_and_graph_equals_direct():
     spec = VARIANTS["dam_break_16k"]
     a = _step(spec, fused=True)[2]
