@@ -207,9 +207,6 @@ __device__ __forceinline__ float cc_sum(float v)
 
 /* widest search half-width whose bucket rows the contact walk loads together */
 #define FG_CONTACT_ROW_MAX 2
-#ifndef FG_CONTACT_ROWS
-#define FG_CONTACT_ROWS 1
-#endif
 
 /* Whether a fluid particle lies outside the bodies' AABB of its scene grown
  * by the contact distance: its contact sum is then exactly zero. */
@@ -248,7 +245,6 @@ __device__ __forceinline__ float3 fg_fluid_rigid_contact(const FgScene *S, uint3
             fg_contact(acc, P, V, q, vq, mind, S->ck, S->ckd);
         }
     };
-#if FG_CONTACT_ROWS
     if (rx >= 0 && rx <= FG_CONTACT_ROW_MAX) {
         /* the same buckets in the same order, with the x hashes computed
          * once and each x row's bucket ranges loaded together: a particle
@@ -280,23 +276,15 @@ __device__ __forceinline__ float3 fg_fluid_rigid_contact(const FgScene *S, uint3
         }
         return acc;
     }
-#endif
+    /* wider half-widths: one bucket at a time */
     for (int z = -rz; z <= rz; z++) {
         const uint32_t hz = fg_axis_hash_rel(p.z, S->rb_cell[2], z, FG_PZ);
         for (int y = -ry; y <= ry; y++) {
             const uint32_t hy = fg_axis_hash_rel(p.y, S->rb_cell[1], y, FG_PY);
             for (int x = -rx; x <= rx; x++) {
-                const uint32_t hx = fg_axis_hash_rel(p.x, S->rb_cell[0], x, FG_PX);
-                const uint32_t b = G.own_geometry ? fg_bucket(hx, hy, hz, G.nb, G.mask)
-                                                  : S->rb_bucket_base + fg_bucket(hx, hy, hz, S->rb_nb, S->rb_nb_mask);
+                const uint32_t b = bucket(fg_axis_hash_rel(p.x, S->rb_cell[0], x, FG_PX), hy, hz);
                 const uint32_t st = __ldg(G.start + b);
-                if (st == FG_EMPTY) continue;
-                const uint32_t en = __ldg(G.end + b);
-                for (uint32_t j = st; j < en; j++) {
-                    const float4 q = __ldg(G.spos + j);
-                    const float4 vq = dynamic ? __ldg(G.body_vel + (int)q.w) : make_float4(0.f, 0.f, 0.f, 0.f);
-                    fg_contact(acc, P, V, q, vq, mind, S->ck, S->ckd);
-                }
+                if (st != FG_EMPTY) visit(st, __ldg(G.end + b));
             }
         }
     }

@@ -8,6 +8,8 @@ Tolerances:
   body force/torque   : FP64 sum of the GPU's per-sphere values, rtol 1e-12
   body state (FP64)   : rtol 1e-12 (same arithmetic, reassociation only)
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -101,8 +103,12 @@ def test_sphere_contact_from_fluid(nbodies):
     assert np.array_equal(Fg[:, 3], F[:, 3]) and np.array_equal(Tg[:, 3], Tq[:, 3])  # w = body index
 
 
-def test_fluid_forces_with_rigid_contact():
-    spec = rigid_scene(nbodies=2)
+@pytest.mark.parametrize("rel", [(2, 2, 2), (1, 1, 1), (1, 3, 2), (3, 1, 2)])
+def test_fluid_forces_with_rigid_contact(rel):
+    """the fluid-side contact term at several search half-widths: the
+    row-batched rigid walk (x half-width up to 2) and the bucket-at-a-time
+    walk (wider)"""
+    spec = dataclasses.replace(rigid_scene(nbodies=2), f2r_rel=rel)
     pos0, v0, before, g = _run(spec)
     r = _rb_grid_ref(spec, before)
     fl = T.oracle_grid(spec, pos0, v0)
