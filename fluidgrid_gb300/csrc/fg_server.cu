@@ -218,9 +218,9 @@ int Server::relayout()
          * lists do not grow (denser particles walk their buckets instead) */
         nw->list_autogrow = false;
         nw->list_cap_alloc = lc;
-        /* the resident set changes every few steps: a Morton target order
-         * rebuilt at each re-layout would land in the step latency */
-        nw->use_order = false;
+        /* the force pass in Morton target order, the density pass in bucket
+         * order (the world default): each re-layout rebuilds the order in its
+         * next step (~0.1 ms), which the faster force pass repays */
         /* trials of slower launch shapes would land in the step latency */
         nw->tune_period = (uint32_t)std::max(cfg.autotune_period, 0);
         if (w) {

@@ -187,7 +187,7 @@ int fg_world_set_graphs(fg_world *w, int on);
  *   FG_OPT_NEIGHBOR_LIST  1 = kernel 1, 0 = kernel 0
  *   FG_OPT_TARGET_ORDER   kernels 0/1: 1 = targets in Morton order of their
  *                         cells, 0 = hashed bucket order, 2 = Morton order in
- *                         the force pass only (default; server worlds 0): the
+ *                         the force pass only (default, server worlds too): the
  *                         density pass walks in bucket order, where a warp's
  *                         lanes share their buckets, and the force pass's
  *                         lanes, spatially close, share neighbour records
